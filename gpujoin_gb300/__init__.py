@@ -1,0 +1,500 @@
+"""gpujoin_gb300 -- GB300-native index-nested-loop-join probe engine.
+
+Python host mirror of the reference's index/operator API (josefschmeisser/
+gpujoin ``src/indexes.cuh``, ``src/indexes.hpp``, ``src/index_lookup_config.hpp``,
+``src/partitioned_relation.hpp``) over the C ABI of ``libgpujoin.so``
+(declared in ``include/gpujoin.h``).  All compute runs in the hand-written
+sm_103a kernels of that library; there is no CPU fallback: if the library
+cannot be loaded, every entry point raises.
+
+Device buffers are torch CUDA tensors.  uint64 columns are carried in int64
+tensors (same bits) and uint32 positions in int32 tensors;
+``INVALID_POS`` (0xFFFFFFFF) therefore reads as -1 in an int32 tensor.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import os
+from typing import Optional, Tuple
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgpujoin.so")
+
+INVALID_POS = 0xFFFFFFFF
+
+GJ_OK = 0
+_ERRORS = {
+    1: "invalid argument",
+    2: "CUDA error",
+    3: "unsupported",
+    4: "out of memory",
+    5: "timeout",
+    6: "unsorted build keys",
+    7: "workspace too small",
+    8: "size exceeds limit",
+}
+
+DIST_UNIFORM = 0
+DIST_LOGNORMAL = 1
+DIST_CLUSTERS = 2
+
+LEARNED_ROOT_LINEAR = 0
+LEARNED_ROOT_MLP = 1
+
+
+class GJError(RuntimeError):
+    """A non-zero status from the C ABI (code, message from gj_last_error_string)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERRORS.get(code, 'error')} ({code}): {message}")
+        self.code = code
+
+
+class index_type_enum(enum.IntEnum):
+    """src/indexes.hpp:5, plus the learned index."""
+
+    btree = 0
+    harmonia = 1
+    binary_search = 2
+    radix_spline = 3
+    no_op = 4
+    learned = 5
+
+
+class gj_index_params(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("btree_node_keys", ctypes.c_uint32),
+        ("rs_radix_bits", ctypes.c_uint32),
+        ("rs_max_error", ctypes.c_uint32),
+        ("bs_cache_keys", ctypes.c_uint32),
+        ("smem_cache_bytes", ctypes.c_uint32),
+        ("learned_leaves", ctypes.c_uint32),
+        ("learned_root", ctypes.c_uint32),
+        ("learned_hidden", ctypes.c_uint32),
+        ("learned_steps", ctypes.c_uint32),
+        ("learned_batch", ctypes.c_uint32),
+        ("learned_lr", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+_LIB: Optional[ctypes.CDLL] = None
+_vp = ctypes.c_void_p
+_u64 = ctypes.c_uint64
+_u32 = ctypes.c_uint32
+_i32 = ctypes.c_int
+_sz = ctypes.c_size_t
+
+_SIGNATURES = {
+    "gj_abi_version": (_u32, []),
+    "gj_last_error_string": (ctypes.c_char_p, []),
+    "gj_index_params_default": (None, [ctypes.POINTER(gj_index_params)]),
+    "gj_parse_index_type": (_i32, [ctypes.c_char_p, ctypes.POINTER(_i32)]),
+    "gj_index_type_name": (ctypes.c_char_p, [_i32]),
+    "gj_index_build": (_i32, [_i32, _vp, _vp, _u64, ctypes.POINTER(gj_index_params), _vp, ctypes.POINTER(_vp)]),
+    "gj_index_free": (_i32, [_vp]),
+    "gj_index_memory_consumption": (_u64, [_vp]),
+    "gj_index_get_type": (_i32, [_vp, ctypes.POINTER(_i32)]),
+    "gj_index_size": (_u64, [_vp]),
+    "gj_index_learned_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)]),
+    "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
+    "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
+    "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
+    "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
+    "gj_partitioned_inlj_workspace_size": (_i32, [_vp, _u64, _u32, ctypes.POINTER(_sz)]),
+    "gj_partitioned_inlj": (_i32, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "gj_star_join_sum": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
+    "gj_batch_lookup": (_i32, [ctypes.POINTER(_vp), _u32, _vp, _vp, _vp, _u32, _vp, _vp, _u32, _vp, _vp, _sz, _vp]),
+    "gj_batch_workspace_size": (_i32, [_u32, _u32, ctypes.POINTER(_sz)]),
+    "gj_generate_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
+    "gj_generate_sorted_keys": (_i32, [_vp, _u64, _u32, _u64, _u64, _vp, _sz, _vp]),
+    "gj_generate_probes": (_i32, [_vp, _u64, _vp, _u64, ctypes.c_double, ctypes.c_double, _u64, _vp]),
+}
+
+
+def exported_symbols():
+    """Names of every C entry point this module binds (all declared in include/gpujoin.h)."""
+    return list(_SIGNATURES)
+
+
+def lib() -> ctypes.CDLL:
+    """Load libgpujoin.so (building it first if it is missing).  Raises if unavailable."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build as _build
+
+            _build.build()
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(rc: int) -> None:
+    if rc != GJ_OK:
+        msg = lib().gj_last_error_string()
+        raise GJError(rc, msg.decode() if msg else "")
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _stream(stream=None) -> int:
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream
+
+
+def _ptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def _empty(n: int, dtype, device):
+    torch = _torch()
+    return torch.empty(n, dtype=dtype, device=device)
+
+
+def _workspace(nbytes: int, device):
+    torch = _torch()
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+def parse_index_type(name: str) -> index_type_enum:
+    """parse_index_type (src/indexes.cpp:5-19); raises RuntimeError("unknown index type")."""
+    out = _i32(0)
+    rc = lib().gj_parse_index_type(name.encode(), ctypes.byref(out))
+    if rc != GJ_OK:
+        raise RuntimeError("unknown index type")
+    return index_type_enum(out.value)
+
+
+def default_params(**overrides) -> gj_index_params:
+    p = gj_index_params()
+    lib().gj_index_params_default(ctypes.byref(p))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise AttributeError(f"unknown index parameter {k}")
+        setattr(p, k, v)
+    return p
+
+
+# --------------------------------------------------------------------------
+# indexes (src/indexes.cuh)
+# --------------------------------------------------------------------------
+class abstract_index:
+    """abstract_index<Key> (src/indexes.cuh:30-39) over a device column of uint64 keys."""
+
+    index_type: index_type_enum = index_type_enum.no_op
+
+    def __init__(self, **params):
+        self.params = default_params(**params)
+        self._handle = _vp(None)
+        self.d_column = None
+
+    # construct(h_column, d_column) -- src/indexes.cuh:36
+    def construct(self, h_column, d_column, stream=None) -> "abstract_index":
+        torch = _torch()
+        if d_column is None or not d_column.is_cuda:
+            raise ValueError("d_column must be a CUDA tensor")
+        if d_column.dtype not in (torch.int64, getattr(torch, "uint64", torch.int64)):
+            raise ValueError("d_column must hold 64-bit keys")
+        self.free()
+        h_ptr = None
+        if h_column is not None:
+            import numpy as np
+
+            self._h_column = np.ascontiguousarray(h_column, dtype=np.uint64)
+            h_ptr = self._h_column.ctypes.data
+        with torch.cuda.device(d_column.device):
+            _check(lib().gj_index_build(int(self.index_type), _ptr(d_column), h_ptr, d_column.numel(),
+                                        ctypes.byref(self.params), _stream(stream), ctypes.byref(self._handle)))
+        self.d_column = d_column
+        self._h_column = None
+        return self
+
+    def memory_consumption(self) -> int:
+        """src/indexes.cuh:38"""
+        return int(lib().gj_index_memory_consumption(self._handle))
+
+    @property
+    def handle(self) -> int:
+        if not self._handle.value:
+            raise RuntimeError("index not constructed")
+        return self._handle.value
+
+    @property
+    def size(self) -> int:
+        return int(lib().gj_index_size(self._handle)) if self._handle.value else 0
+
+    def type_name(self) -> str:
+        return lib().gj_index_type_name(int(self.index_type)).decode()
+
+    # ---- probe operators ------------------------------------------------
+    def lookup(self, d_probes, out=None, stream=None):
+        """Plain INLJ probe (lookup_kernel, src/index_lookup_common.cuh:217-245) -> int32 positions."""
+        torch = _torch()
+        m = d_probes.numel()
+        if out is None:
+            out = _empty(m, torch.int32, d_probes.device)
+        _check(lib().gj_index_lookup(self.handle, _ptr(d_probes), m, _ptr(out), _stream(stream)))
+        return out
+
+    def inlj_pairs(self, d_probes, out_pairs=None, out_count=None, workspace=None, stream=None):
+        """(probe row, build pos) pairs of the matches, in probe order (ij_lookup_kernel)."""
+        torch = _torch()
+        m = d_probes.numel()
+        dev = d_probes.device
+        if out_pairs is None:
+            out_pairs = _empty(2 * max(m, 1), torch.int32, dev)
+        if out_count is None:
+            out_count = torch.zeros(1, dtype=torch.int64, device=dev)
+        if workspace is None:
+            need = _sz(0)
+            _check(lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(need)))
+            workspace = _workspace(need.value, dev)
+        _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
+                                   _ptr(workspace), workspace.numel(), _stream(stream)))
+        return out_pairs, out_count
+
+    def partitioned_inlj(self, d_probes, window_size: int = 0, radix_bits: int = 0, positions: bool = True,
+                         pairs: bool = False, workspace=None, stream=None):
+        """Windowed partitioned INLJ (src/index_lookup_partitioning.cu:436-507)."""
+        torch = _torch()
+        m = d_probes.numel()
+        dev = d_probes.device
+        window = window_size if window_size else max(m, 1)
+        pos = _empty(m, torch.int32, dev) if positions else None
+        prs = _empty(2 * max(m, 1), torch.int32, dev) if pairs else None
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev) if pairs else None
+        if workspace is None:
+            need = _sz(0)
+            _check(lib().gj_partitioned_inlj_workspace_size(self.handle, window, radix_bits, ctypes.byref(need)))
+            workspace = _workspace(need.value, dev)
+        _check(lib().gj_partitioned_inlj(self.handle, _ptr(d_probes), m, window, radix_bits, _ptr(pos), _ptr(prs),
+                                         _ptr(cnt), _ptr(workspace), workspace.numel(), _stream(stream)))
+        return pos, prs, cnt
+
+    def partitioned_lookup(self, d_part_keys, d_part_rows, out, stream=None):
+        """partitioned_lookup_kernel (src/index_lookup_partitioning.cu:218-248): out[row] = lookup(key)."""
+        _check(lib().gj_partitioned_lookup(self.handle, _ptr(d_part_keys), _ptr(d_part_rows), d_part_keys.numel(),
+                                           _ptr(out), _stream(stream)))
+        return out
+
+    def free(self) -> None:
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            _check(lib().gj_index_free(self._handle))
+            self._handle = _vp(None)
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class btree_index(abstract_index):
+    """btree_index (src/indexes.cuh:93-147): clustered B+tree, 64-key nodes by default."""
+
+    index_type = index_type_enum.btree
+
+
+class harmonia_index(abstract_index):
+    """harmonia_index (src/indexes.cuh:257-307): column size must be a multiple of 32."""
+
+    index_type = index_type_enum.harmonia
+
+
+class binary_search_index(abstract_index):
+    """binary_search_index (src/indexes.cuh:336-375): lower bound, INVALID_POS at n."""
+
+    index_type = index_type_enum.binary_search
+
+
+class radix_spline_index(abstract_index):
+    """radix_spline_index (src/indexes.cuh:176-248): 18 radix bits, spline error 32 by default."""
+
+    index_type = index_type_enum.radix_spline
+
+
+class no_op_index(abstract_index):
+    """no_op_index (src/indexes.cuh:384-406): every probe returns INVALID_POS."""
+
+    index_type = index_type_enum.no_op
+
+    def construct(self, h_column, d_column, stream=None):
+        torch = _torch()
+        if d_column is None:
+            d_column = torch.empty(0, dtype=torch.int64, device="cuda")
+        return super().construct(h_column, d_column, stream)
+
+
+class learned_index(abstract_index):
+    """Trained position model (root + linear leaves) with an exact bounded search."""
+
+    index_type = index_type_enum.learned
+
+    def stats(self) -> Tuple[int, float]:
+        me = _u64(0)
+        mw = ctypes.c_double(0)
+        _check(lib().gj_index_learned_stats(self.handle, ctypes.byref(me), ctypes.byref(mw)))
+        return int(me.value), float(mw.value)
+
+
+_INDEX_CLASSES = {
+    index_type_enum.btree: btree_index,
+    index_type_enum.harmonia: harmonia_index,
+    index_type_enum.binary_search: binary_search_index,
+    index_type_enum.radix_spline: radix_spline_index,
+    index_type_enum.no_op: no_op_index,
+    index_type_enum.learned: learned_index,
+}
+
+
+def make_index(kind, **params) -> abstract_index:
+    """Index object for an index_type_enum value or a reference index name."""
+    if isinstance(kind, str):
+        kind = parse_index_type(kind)
+    return _INDEX_CLASSES[index_type_enum(kind)](**params)
+
+
+# --------------------------------------------------------------------------
+# partitioning (src/partitioned_relation.hpp, src/index_lookup_partitioning.cu)
+# --------------------------------------------------------------------------
+@dataclasses.dataclass
+class partitioned_relation:
+    """partitioned_relation<T> (src/partitioned_relation.hpp:27-50) in SoA form:
+    keys / rows of the partitioned tuples and the start offset of each partition."""
+
+    keys: object
+    rows: object
+    offsets: object
+    radix_bits: int
+
+    @property
+    def fanout(self) -> int:
+        return 1 << self.radix_bits
+
+
+def range_partition(d_keys, min_key: int, shift: int, radix_bits: int, workspace=None,
+                    stream=None) -> partitioned_relation:
+    torch = _torch()
+    m = d_keys.numel()
+    dev = d_keys.device
+    out_k = _empty(max(m, 1), torch.int64, dev)
+    out_r = _empty(max(m, 1), torch.int32, dev)
+    offs = _empty((1 << radix_bits) + 1, torch.int64, dev)
+    if workspace is None:
+        need = _sz(0)
+        _check(lib().gj_partition_workspace_size(m, radix_bits, ctypes.byref(need)))
+        workspace = _workspace(need.value, dev)
+    _check(lib().gj_range_partition(_ptr(d_keys), m, min_key, shift, radix_bits, _ptr(out_k), _ptr(out_r), _ptr(offs),
+                                    _ptr(workspace), workspace.numel(), _stream(stream)))
+    return partitioned_relation(out_k[:m], out_r[:m], offs, radix_bits)
+
+
+# --------------------------------------------------------------------------
+# star join (src/tpch/tpch_14_ij.cu, src/tpch/cpu_only.cpp:230-275)
+# --------------------------------------------------------------------------
+def star_join_sum(dim_index: abstract_index, d_fk, d_date, d_price, d_discount, d_dim_flag, lo: int, hi: int,
+                  out=None, stream=None):
+    """Returns a 2-element int64 tensor [sum over flagged rows, sum over all rows]."""
+    torch = _torch()
+    if out is None:
+        out = torch.zeros(2, dtype=torch.int64, device=d_fk.device)
+    _check(lib().gj_star_join_sum(dim_index.handle, _ptr(d_fk), _ptr(d_date), _ptr(d_price), _ptr(d_discount),
+                                  d_fk.numel(), _ptr(d_dim_flag), lo, hi, _ptr(out), _stream(stream)))
+    return out
+
+
+# --------------------------------------------------------------------------
+# batched lookup stream
+# --------------------------------------------------------------------------
+def batch_lookup(indexes, batch_index, probe_offset, batch_size, d_probes, d_positions, mode: int = 0,
+                 d_done_ns=None, workspace=None, stream=None):
+    """Many probe batches against several indexes; mode 0 = one persistent kernel, 1 = one launch per batch."""
+    import numpy as np
+
+    nb = len(batch_index)
+    arr_t = _vp * len(indexes)
+    handles = arr_t(*[ix.handle for ix in indexes])
+    bi = np.ascontiguousarray(batch_index, dtype=np.uint32)
+    po = np.ascontiguousarray(probe_offset, dtype=np.uint64)
+    bs = np.ascontiguousarray(batch_size, dtype=np.uint64)
+    dev = d_probes.device
+    if workspace is None:
+        need = _sz(0)
+        _check(lib().gj_batch_workspace_size(len(indexes), nb, ctypes.byref(need)))
+        workspace = _workspace(need.value, dev)
+    _check(lib().gj_batch_lookup(handles, len(indexes), bi.ctypes.data, po.ctypes.data, bs.ctypes.data, nb,
+                                 _ptr(d_probes), _ptr(d_positions), mode, _ptr(d_done_ns), _ptr(workspace),
+                                 workspace.numel(), _stream(stream)))
+    return d_positions
+
+
+# --------------------------------------------------------------------------
+# synthetic inputs (src/index_lookup_common.cuh:44-206)
+# --------------------------------------------------------------------------
+def generate_sorted_keys(n: int, distribution: int = DIST_UNIFORM, upper: int = 1 << 63, seed: int = 1,
+                         device="cuda", stream=None):
+    torch = _torch()
+    out = _empty(max(n, 1), torch.int64, device)
+    need = _sz(0)
+    _check(lib().gj_generate_workspace_size(n, ctypes.byref(need)))
+    ws = _workspace(need.value, out.device)
+    _check(lib().gj_generate_sorted_keys(_ptr(out), n, distribution, upper, seed, _ptr(ws), ws.numel(),
+                                         _stream(stream)))
+    return out[:n]
+
+
+def generate_probes(d_keys, m: int, theta: float = 0.0, absent_fraction: float = 0.0, seed: int = 2, stream=None):
+    torch = _torch()
+    out = _empty(max(m, 1), torch.int64, d_keys.device)
+    _check(lib().gj_generate_probes(_ptr(d_keys), d_keys.numel(), _ptr(out), m, float(theta), float(absent_fraction),
+                                    seed, _stream(stream)))
+    return out[:m]
+
+
+# --------------------------------------------------------------------------
+# experiment configuration (src/index_lookup_config.hpp:18-37)
+# --------------------------------------------------------------------------
+@dataclasses.dataclass
+class experiment_config:
+    approach: str = "plain"
+    index_type: str = "btree"
+    scenario: str = "single"
+    output_file: str = ""
+    num_lookups: int = int(1e8)
+    num_elements: int = int(1e6)
+    max_bits: int = 0
+    zipf_factor: float = 1.25
+    block_size: int = 128
+    dataset: str = "sparse"
+    lookup_pattern: str = "uniform"
+    sorted_lookups: bool = False
+    partitioning_approach_ignore_bits: int = 4
+    partitioning_approach_dynamic_bit_range: bool = True
+    partitioning_approach_window_size: int = 10000
+
+
+radix_bits = 11  # src/index_lookup_config.hpp:37 (the reference's fixed fanout)

@@ -1,0 +1,477 @@
+// gj_index.cu -- C ABI: library state, index construction and the probe
+// entry points.
+//
+// Index construction replaces abstract_index::construct and its overrides
+// (src/indexes.cuh:36,126,218,285,364); every index borrows the caller's
+// device column as the reference's binary_search_index / radix_spline_index
+// do, and the B+tree and Harmonia use it as their leaf level.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gj_internal.h"
+
+namespace gj {
+
+// ---------------------------------------------------------------------------
+// errors and device properties
+// ---------------------------------------------------------------------------
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+const char* last_error() { return g_last_error.c_str(); }
+
+int current_device_info(device_info* out) {
+    static device_info cache[64];
+    int dev = 0;
+    GJ_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return GJ_ERR_UNSUPPORTED;
+    }
+    if (cache[dev].device != dev) {
+        device_info di;
+        di.device = dev;
+        GJ_CUDA_TRY(cudaDeviceGetAttribute(&di.sm_count, cudaDevAttrMultiProcessorCount, dev));
+        int v = 0;
+        GJ_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        di.smem_optin = (size_t)v;
+        GJ_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev));
+        di.l2_bytes = (size_t)v;
+        cache[dev] = di;
+    }
+    *out = cache[dev];
+    return GJ_OK;
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// build kernels
+// ---------------------------------------------------------------------------
+__global__ void k_count_unsorted(const uint64_t* __restrict__ col, uint64_t n, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < n; i += (uint64_t)gridDim.x * blockDim.x)
+        local += (col[i] >= col[i + 1]);
+    if (local) atomicAdd(bad, local);
+}
+
+// fence[j] = col[j << shift] for j < used, UINT64_MAX up to slots
+__global__ void k_gather_fence(const uint64_t* __restrict__ col, uint64_t n, uint32_t shift, uint32_t slots,
+                               uint64_t* __restrict__ fence) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < slots; j += gridDim.x * blockDim.x) {
+        const uint64_t p = (uint64_t)j << shift;
+        fence[j] = p < n ? col[p] : UINT64_MAX;
+    }
+}
+
+// B+tree level l: slot k = max key of child k at level l-1, which covers the
+// column range [k * span, (k + 1) * span) with span = W^l
+__global__ void k_gather_btree_level(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint64_t slots,
+                                     uint64_t* __restrict__ level) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < slots; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t first = k * span;
+        if (first < n) {
+            uint64_t last = first + span;
+            if (last > n) last = n;
+            level[k] = col[last - 1];
+        } else {
+            level[k] = UINT64_MAX;
+        }
+    }
+}
+
+int device_alloc(gj_index* idx, size_t bytes, void** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? GJ_ERR_OUT_OF_MEMORY : GJ_ERR_CUDA;
+    }
+    idx->allocations.push_back(p);
+    *out = p;
+    return GJ_OK;
+}
+
+int host_copy_of_column(const uint64_t* d_keys, const uint64_t* h_keys, uint64_t n, std::vector<uint64_t>* store,
+                        const uint64_t** out) {
+    if (h_keys) {
+        *out = h_keys;
+        return GJ_OK;
+    }
+    store->resize(n);
+    GJ_CUDA_TRY(cudaMemcpy(store->data(), d_keys, n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    *out = store->data();
+    return GJ_OK;
+}
+
+int build_binary_search(gj_index* idx, cudaStream_t s) {
+    idx->bs.col = idx->d_col;
+    idx->bs.n = idx->n;
+    const uint32_t want = idx->params.bs_cache_keys;
+    if (want == 0 || idx->n < 64) return GJ_OK;
+    // slots: a power of two <= want; stride 2^shift with slots * 2^shift >= n
+    uint32_t slots = 1;
+    while ((slots << 1) <= want && (slots << 1) != 0) slots <<= 1;
+    uint32_t shift = 0;
+    while (((uint64_t)slots << shift) < idx->n) ++shift;
+    // do not sample finer than needed
+    while (slots > 2 && ((uint64_t)(slots >> 1) << shift) >= idx->n) slots >>= 1;
+    uint32_t steps = 0;
+    while ((1u << steps) < slots) ++steps;
+    void* p = nullptr;
+    GJ_TRY(device_alloc(idx, (size_t)slots * sizeof(uint64_t), &p));
+    k_gather_fence<<<(slots + 255) / 256, 256, 0, s>>>(idx->d_col, idx->n, shift, slots, static_cast<uint64_t*>(p));
+    GJ_CUDA_TRY(cudaGetLastError());
+    idx->bs.fence = static_cast<uint64_t*>(p);
+    idx->bs.fence_slots = slots;
+    idx->bs.fence_shift = shift;
+    idx->bs.fence_steps = steps;
+    idx->bytes = (uint64_t)slots * sizeof(uint64_t);
+    return GJ_OK;
+}
+
+int build_btree(gj_index* idx, cudaStream_t s) {
+    const uint32_t W = idx->params.btree_node_keys;
+    uint32_t logw = 0;
+    while ((1u << logw) < W) ++logw;
+    if ((1u << logw) != W || logw < 4 || logw > 6) {
+        set_error("btree: node size must be 16, 32 or 64 keys (got %u)", W);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    const uint64_t n = idx->n;
+    // level sizes: level l has ceil(n / W^(l+1)) nodes; stop at one node
+    std::vector<uint64_t> nodes(1, 0);
+    uint64_t span = W;  // keys below one slot of level 1
+    for (int l = 1;; ++l) {
+        if (l >= kBtreeMaxLevels) {
+            set_error("btree: more than %d levels", kBtreeMaxLevels - 1);
+            return GJ_ERR_UNSUPPORTED;
+        }
+        const uint64_t node_span = span * W;  // keys below one node
+        const uint64_t cnt = (n + node_span - 1) / node_span;
+        nodes.push_back(cnt);
+        if (cnt == 1) break;
+        span = node_span;
+    }
+    const uint32_t height = (uint32_t)nodes.size() - 1;
+    // storage: top level first so that the shared-memory cache is a prefix
+    std::vector<uint64_t> offset(height + 1, 0);
+    uint64_t total = 0;
+    for (uint32_t l = height; l >= 1; --l) {
+        offset[l] = total;
+        total += nodes[l] * W;
+    }
+    void* p = nullptr;
+    GJ_TRY(device_alloc(idx, total * sizeof(uint64_t), &p));
+    uint64_t* base = static_cast<uint64_t*>(p);
+    span = W;
+    for (uint32_t l = 1; l <= height; ++l) {
+        const uint64_t slots = nodes[l] * W;
+        const int grid = (int)std::min<uint64_t>((slots + 255) / 256, 65535);
+        k_gather_btree_level<<<grid, 256, 0, s>>>(idx->d_col, n, span, slots, base + offset[l]);
+        GJ_CUDA_TRY(cudaGetLastError());
+        idx->bt.level[l] = base + offset[l];
+        span *= W;
+    }
+    // shared-memory cache: as many top levels as fit the budget
+    uint32_t cached = 0;
+    uint64_t cache_keys = 0;
+    for (uint32_t l = height; l >= 1; --l) {
+        const uint64_t add = nodes[l] * W;
+        if ((cache_keys + add) * sizeof(uint64_t) > idx->params.smem_cache_bytes) break;
+        cache_keys += add;
+        cached += 1;
+        idx->bt.smem_offset[l] = (uint32_t)offset[l];
+    }
+    idx->bt.col = idx->d_col;
+    idx->bt.n = n;
+    idx->bt.height = height;
+    idx->bt.cached_levels = cached;
+    idx->bt.cache_keys = (uint32_t)cache_keys;
+    idx->bt.node_keys = W;
+    idx->bt_logw = logw;
+    uint64_t maxk = 0;
+    GJ_CUDA_TRY(cudaMemcpyAsync(&maxk, idx->d_col + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    idx->bt.max_key = maxk;
+    idx->bytes = total * sizeof(uint64_t);
+    return GJ_OK;
+}
+
+int build_harmonia(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
+    if (idx->n % kHarmoniaKeys != 0) {
+        set_error("harmonia: when Reuse_Input_Memory is set the dataset set must be a multiple of the node size "
+                  "(n = %llu, node size %d)", (unsigned long long)idx->n, kHarmoniaKeys);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<uint64_t> store;
+    const uint64_t* col = nullptr;
+    GJ_TRY(host_copy_of_column(idx->d_col, h_keys, idx->n, &store, &col));
+    harmonia_arrays ha;
+    GJ_TRY(build_harmonia_arrays(col, idx->n, &ha));
+    void *pk = nullptr, *pc = nullptr;
+    GJ_TRY(device_alloc(idx, ha.keys.size() * sizeof(uint64_t), &pk));
+    GJ_TRY(device_alloc(idx, ha.children.size() * sizeof(uint64_t), &pc));
+    if (!ha.keys.empty())
+        GJ_CUDA_TRY(cudaMemcpyAsync(pk, ha.keys.data(), ha.keys.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(pc, ha.children.data(), ha.children.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    idx->hm.keys = static_cast<uint64_t*>(pk);
+    idx->hm.children = static_cast<uint64_t*>(pc);
+    idx->hm.col = idx->d_col;
+    idx->hm.n = idx->n;
+    idx->hm.inner_size = ha.keys.size();
+    idx->hm.depth = ha.depth;
+    const uint64_t inner_nodes = ha.keys.size() / kHarmoniaKeys;
+    const uint64_t per_node = (kHarmoniaKeys + 1) * sizeof(uint64_t);
+    uint64_t cached = idx->params.smem_cache_bytes / per_node;
+    if (cached > inner_nodes) cached = inner_nodes;
+    idx->hm.cached_nodes = (uint32_t)cached;
+    idx->bytes = (ha.keys.size() + ha.children.size()) * sizeof(uint64_t);
+    return GJ_OK;
+}
+
+int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
+    std::vector<uint64_t> store;
+    const uint64_t* col = nullptr;
+    GJ_TRY(host_copy_of_column(idx->d_col, h_keys, idx->n, &store, &col));
+    radix_spline_arrays rs;
+    GJ_TRY(build_radix_spline(col, idx->n, idx->params.rs_radix_bits, idx->params.rs_max_error, &rs));
+    void *pt = nullptr, *px = nullptr, *py = nullptr;
+    GJ_TRY(device_alloc(idx, rs.table.size() * sizeof(uint32_t), &pt));
+    GJ_TRY(device_alloc(idx, rs.sx.size() * sizeof(uint64_t), &px));
+    GJ_TRY(device_alloc(idx, rs.sy.size() * sizeof(double), &py));
+    GJ_CUDA_TRY(cudaMemcpyAsync(pt, rs.table.data(), rs.table.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(px, rs.sx.data(), rs.sx.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(py, rs.sy.data(), rs.sy.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    idx->rs.col = idx->d_col;
+    idx->rs.n = idx->n;
+    idx->rs.table = static_cast<uint32_t*>(pt);
+    idx->rs.sx = static_cast<uint64_t*>(px);
+    idx->rs.sy = static_cast<double*>(py);
+    idx->rs.min_key = rs.min_key;
+    idx->rs.max_key = rs.max_key;
+    idx->rs.shift = rs.shift;
+    idx->rs.max_error = idx->params.rs_max_error;
+    idx->bytes = rs.table.size() * sizeof(uint32_t) + rs.sx.size() * (sizeof(uint64_t) + sizeof(double));
+    return GJ_OK;
+}
+
+}  // namespace
+
+int build_learned(gj_index* idx, cudaStream_t s);  // gj_learned.cu
+
+}  // namespace gj
+
+using namespace gj;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+uint32_t gj_abi_version(void) { return GJ_ABI_VERSION; }
+
+const char* gj_last_error_string(void) { return gj::last_error(); }
+
+void gj_index_params_default(gj_index_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->struct_size = sizeof(gj_index_params);
+    p->btree_node_keys = 64;
+    p->rs_radix_bits = 18;
+    p->rs_max_error = 32;
+    p->bs_cache_keys = 4096;
+    p->smem_cache_bytes = 16384;
+    p->learned_leaves = 16384;
+    p->learned_root = GJ_LEARNED_ROOT_MLP;
+    p->learned_hidden = 32;
+    p->learned_steps = 600;
+    p->learned_batch = 8192;
+    p->learned_lr = 3e-3f;
+    p->seed = 0x5eedULL;
+}
+
+int gj_parse_index_type(const char* name, int* out_type) {
+    GJ_CHECK_ARG(name && out_type, "gj_parse_index_type: null argument");
+    static const struct {
+        const char* name;
+        int type;
+    } table[] = {{"btree", GJ_INDEX_BTREE},
+                 {"harmonia", GJ_INDEX_HARMONIA},
+                 {"binary_search", GJ_INDEX_BINARY_SEARCH},
+                 {"radix_spline", GJ_INDEX_RADIX_SPLINE},
+                 {"no_op", GJ_INDEX_NO_OP},
+                 {"learned", GJ_INDEX_LEARNED}};
+    for (const auto& e : table) {
+        if (std::strcmp(name, e.name) == 0) {
+            *out_type = e.type;
+            return GJ_OK;
+        }
+    }
+    set_error("unknown index type");
+    return GJ_ERR_INVALID_ARGUMENT;
+}
+
+const char* gj_index_type_name(int type) {
+    switch (type) {
+        case GJ_INDEX_BTREE: return "btree";
+        case GJ_INDEX_HARMONIA: return "harmonia";
+        case GJ_INDEX_BINARY_SEARCH: return "binary_search";
+        case GJ_INDEX_RADIX_SPLINE: return "radix_spline";
+        case GJ_INDEX_NO_OP: return "no_op";
+        case GJ_INDEX_LEARNED: return "learned";
+        default: return nullptr;
+    }
+}
+
+int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uint64_t n,
+                   const gj_index_params* params, void* stream, gj_index** out_index) {
+    GJ_CHECK_ARG(out_index, "gj_index_build: out_index is null");
+    *out_index = nullptr;
+    GJ_CHECK_ARG(gj_index_type_name(type) != nullptr, "gj_index_build: unknown index type");
+    GJ_CHECK_ARG(d_keys || type == GJ_INDEX_NO_OP, "gj_index_build: d_keys is null");
+    if (type != GJ_INDEX_NO_OP && n == 0) {
+        set_error("gj_index_build: empty column");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (n >= (uint64_t)GJ_INVALID_POS) {
+        set_error("'value_t' does not suffice: %llu keys do not fit 32-bit positions", (unsigned long long)n);
+        return GJ_ERR_TOO_LARGE;
+    }
+    gj_index_params p;
+    gj_index_params_default(&p);
+    if (params) {
+        GJ_CHECK_ARG(params->struct_size == sizeof(gj_index_params), "gj_index_build: params.struct_size mismatch");
+        p = *params;
+    }
+    cudaStream_t s = as_stream(stream);
+    std::unique_ptr<gj_index> idx(new gj_index());
+    idx->type = type;
+    idx->n = n;
+    idx->d_col = d_keys;
+    idx->params = p;
+    GJ_CUDA_TRY(cudaGetDevice(&idx->device));
+
+    if (type != GJ_INDEX_NO_OP && n > 1) {
+        unsigned long long* d_bad = nullptr;
+        GJ_CUDA_TRY(cudaMallocAsync(&d_bad, sizeof(unsigned long long), s));
+        cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), s);
+        const int grid = (int)std::min<uint64_t>((n + 255) / 256, 4096);
+        k_count_unsorted<<<grid, 256, 0, s>>>(d_keys, n, d_bad);
+        unsigned long long bad = 0;
+        cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(d_bad, s);
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+        if (bad) {
+            set_error("build keys are not strictly increasing (%llu violations)", bad);
+            return GJ_ERR_UNSORTED;
+        }
+    }
+
+    int rc = GJ_OK;
+    switch (type) {
+        case GJ_INDEX_BINARY_SEARCH: rc = build_binary_search(idx.get(), s); break;
+        case GJ_INDEX_BTREE: rc = build_btree(idx.get(), s); break;
+        case GJ_INDEX_HARMONIA: rc = build_harmonia(idx.get(), h_keys, s); break;
+        case GJ_INDEX_RADIX_SPLINE: rc = build_radix_spline_index(idx.get(), h_keys, s); break;
+        case GJ_INDEX_LEARNED: rc = build_learned(idx.get(), s); break;
+        case GJ_INDEX_NO_OP: break;
+    }
+    if (rc == GJ_OK) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("index build: %s", cudaGetErrorString(e));
+            rc = GJ_ERR_CUDA;
+        }
+    }
+    if (rc != GJ_OK) {
+        for (void* a : idx->allocations) cudaFree(a);
+        return rc;
+    }
+    *out_index = idx.release();
+    return GJ_OK;
+}
+
+int gj_index_free(gj_index* index) {
+    if (!index) return GJ_OK;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != index->device) cudaSetDevice(index->device);
+    int rc = GJ_OK;
+    for (void* a : index->allocations) {
+        cudaError_t e = cudaFree(a);
+        if (e != cudaSuccess && rc == GJ_OK) {
+            set_error("cudaFree: %s", cudaGetErrorString(e));
+            rc = GJ_ERR_CUDA;
+        }
+    }
+    if (prev != index->device && prev >= 0) cudaSetDevice(prev);
+    delete index;
+    return rc;
+}
+
+uint64_t gj_index_memory_consumption(const gj_index* index) { return index ? index->bytes : 0; }
+
+int gj_index_get_type(const gj_index* index, int* out_type) {
+    GJ_CHECK_ARG(index && out_type, "gj_index_get_type: null argument");
+    *out_type = index->type;
+    return GJ_OK;
+}
+
+uint64_t gj_index_size(const gj_index* index) { return index ? index->n : 0; }
+
+int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* mean_window) {
+    GJ_CHECK_ARG(index, "gj_index_learned_stats: null index");
+    if (index->type != GJ_INDEX_LEARNED) {
+        set_error("gj_index_learned_stats: not a learned index");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (max_error) *max_error = index->learned_max_error;
+    if (mean_window) *mean_window = index->learned_mean_window;
+    return GJ_OK;
+}
+
+int gj_index_lookup(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,
+                    void* stream) {
+    GJ_CHECK_ARG(index, "gj_index_lookup: null index");
+    GJ_CHECK_ARG(m == 0 || (d_probes && d_positions), "gj_index_lookup: null buffer");
+    return launch_lookup(index, d_probes, m, d_positions, as_stream(stream));
+}
+
+int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes) {
+    GJ_CHECK_ARG(bytes, "gj_inlj_pairs_workspace_size: null argument");
+    *bytes = pairs_workspace_bytes(m);
+    return GJ_OK;
+}
+
+int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs, uint64_t* d_count,
+                  void* d_workspace, size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(index && d_count, "gj_inlj_pairs: null argument");
+    GJ_CHECK_ARG(m == 0 || (d_probes && d_pairs), "gj_inlj_pairs: null buffer");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_inlj_pairs: probe rows must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    return launch_pairs(index, d_probes, m, nullptr, d_pairs, nullptr, d_count, d_workspace, workspace_bytes,
+                        as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,276 @@
+// gj_partition.cu -- range partitioning of the probe side and the windowed
+// partitioned INLJ.
+//
+// Replaces the fast-interconnects prefix-sum + chunked radix-partition
+// kernels driven by run_on_stream (src/index_lookup_partitioning.cu:300-359)
+// and the window loop of partitioning_approach (:436-507).  The reference
+// partitions on key bits [max_bits - 11, max_bits) (src/index_lookup_new.cu:
+// 63-67); here the partition function is a range split of the index's key
+// range, partition(k) = min((k - min) >> shift, fanout - 1), so each partition
+// maps onto one contiguous slice of the index and a window's lookups walk the
+// index in order (the slices stay resident in the 126 MB L2).
+//
+// Pipeline per window (all on the caller's stream):
+//   1. k_part_hist   per-block histograms of the window's keys
+//   2. scan          exclusive offsets, partition-major (p, block)
+//   3. k_part_scatter keys and row ids to their partition, in block order
+//   4. lookup        scattered positions and/or pairs in partition order
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "gj_internal.h"
+
+namespace gj {
+namespace {
+
+constexpr int kPartBlock = 512;
+constexpr uint32_t kMaxRadixBits = 12;
+
+__device__ __forceinline__ uint32_t part_of(uint64_t key, uint64_t min_key, uint32_t shift, uint32_t fanout) {
+    if (key <= min_key) return 0;
+    const uint64_t p = (key - min_key) >> shift;
+    return p >= fanout ? fanout - 1 : (uint32_t)p;
+}
+
+// hist[p * G + b] = number of keys of block b's chunk in partition p
+__global__ void __launch_bounds__(kPartBlock) k_part_hist(const uint64_t* __restrict__ keys, uint64_t m, uint64_t chunk,
+                                                          uint64_t min_key, uint32_t shift, uint32_t fanout,
+                                                          uint64_t* __restrict__ hist) {
+    extern __shared__ uint32_t s_hist[];
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_hist[p] = 0;
+    __syncthreads();
+    const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+        atomicAdd(&s_hist[part_of(__ldg(reinterpret_cast<const unsigned long long*>(keys) + i), min_key, shift, fanout)], 1u);
+    __syncthreads();
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) hist[(uint64_t)p * gridDim.x + blockIdx.x] = s_hist[p];
+}
+
+// offsets[p] = start of partition p (inclusive scan of hist, read at the
+// previous partition's last block); offsets[fanout] = m
+__global__ void k_part_offsets(const uint64_t* __restrict__ incl, uint32_t fanout, uint32_t nblocks, uint64_t m,
+                               uint64_t* __restrict__ offsets) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= fanout; p += gridDim.x * blockDim.x)
+        offsets[p] = p == 0 ? 0 : (p == fanout ? m : incl[(uint64_t)p * nblocks - 1]);
+}
+
+// scatter block b's chunk; the running offsets start at the exclusive
+// prefix of (p, b).  Ranks inside a block come from shared-memory atomics,
+// so the order inside a partition follows the block order but not the probe
+// order within one block.
+__global__ void __launch_bounds__(kPartBlock) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
+                                                             uint64_t chunk, uint64_t min_key, uint32_t shift,
+                                                             uint32_t fanout, const uint64_t* __restrict__ incl,
+                                                             uint64_t row_base, uint64_t* __restrict__ out_keys,
+                                                             uint32_t* __restrict__ out_rows) {
+    extern __shared__ unsigned long long s_next[];
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_next + fanout);
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_cnt[p] = 0;
+    __syncthreads();
+    const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
+    // this block's own counts, to turn the inclusive scan into its start offsets
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+        atomicAdd(&s_cnt[part_of(__ldg(reinterpret_cast<const unsigned long long*>(keys) + i), min_key, shift, fanout)], 1u);
+    __syncthreads();
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x)
+        s_next[p] = incl[(uint64_t)p * gridDim.x + blockIdx.x] - s_cnt[p];
+    __syncthreads();
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        const uint64_t k = __ldcs(reinterpret_cast<const unsigned long long*>(keys) + i);
+        const uint32_t p = part_of(k, min_key, shift, fanout);
+        const unsigned long long d = atomicAdd(&s_next[p], 1ull);
+        out_keys[d] = k;
+        out_rows[d] = (uint32_t)(row_base + i);
+    }
+}
+
+struct partition_plan {
+    uint32_t fanout, nblocks;
+    uint64_t chunk;
+};
+
+partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
+    partition_plan pl;
+    pl.fanout = 1u << radix_bits;
+    uint64_t nb = (uint64_t)sm_count * 2;
+    const uint64_t min_chunk = 4096;
+    if (nb * min_chunk > m) nb = std::max<uint64_t>(1, (m + min_chunk - 1) / min_chunk);
+    pl.chunk = (m + nb - 1) / nb;
+    pl.nblocks = (uint32_t)((m + pl.chunk - 1) / pl.chunk);
+    if (pl.nblocks == 0) pl.nblocks = 1;
+    return pl;
+}
+
+size_t partition_ws_bytes(uint64_t m, uint32_t radix_bits, int sm_count) {
+    const partition_plan pl = plan_partition(m ? m : 1, radix_bits, sm_count);
+    const uint64_t cells = (uint64_t)pl.fanout * pl.nblocks;
+    return workspace_carver::need({cells * sizeof(uint64_t), scan_workspace_bytes(cells)});
+}
+
+int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift, uint32_t radix_bits,
+                         uint64_t row_base, uint64_t* d_out_keys, uint32_t* d_out_rows, uint64_t* d_offsets, void* ws,
+                         size_t ws_bytes, cudaStream_t s) {
+    device_info di;
+    GJ_TRY(current_device_info(&di));
+    const partition_plan pl = plan_partition(m ? m : 1, radix_bits, di.sm_count);
+    const uint64_t cells = (uint64_t)pl.fanout * pl.nblocks;
+    workspace_carver wc(ws, ws_bytes);
+    uint64_t* hist = wc.take<uint64_t>(cells);
+    void* scan_ws = wc.take<char>(scan_workspace_bytes(cells));
+    if (!hist || !scan_ws) {
+        set_error("range partition: workspace of %zu bytes is smaller than the %zu required", ws_bytes,
+                  partition_ws_bytes(m, radix_bits, di.sm_count));
+        return GJ_ERR_WORKSPACE;
+    }
+    if (m == 0) {
+        if (d_offsets) GJ_CUDA_TRY(cudaMemsetAsync(d_offsets, 0, ((size_t)pl.fanout + 1) * sizeof(uint64_t), s));
+        return GJ_OK;
+    }
+    const size_t smem_hist = pl.fanout * sizeof(uint32_t);
+    const size_t smem_scatter = pl.fanout * (sizeof(unsigned long long) + sizeof(uint32_t));
+    if (smem_scatter > 48 * 1024)
+        GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_scatter));
+    k_part_hist<<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
+    GJ_CUDA_TRY(cudaGetLastError());
+    GJ_TRY(inclusive_scan_sum(hist, cells, scan_ws, scan_workspace_bytes(cells), s));
+    if (d_offsets) {
+        k_part_offsets<<<(pl.fanout + 256) / 256, 256, 0, s>>>(hist, pl.fanout, pl.nblocks, m, d_offsets);
+        GJ_CUDA_TRY(cudaGetLastError());
+    }
+    k_part_scatter<<<pl.nblocks, kPartBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist,
+                                                                row_base, d_out_keys, d_out_rows);
+    GJ_CUDA_TRY(cudaGetLastError());
+    return GJ_OK;
+}
+
+// key range and fanout used by the partitioned INLJ for an index
+int index_key_range(const gj_index* idx, uint64_t* min_key, uint64_t* max_key, cudaStream_t s) {
+    if (idx->n == 0 || !idx->d_col) {
+        *min_key = 0;
+        *max_key = 0;
+        return GJ_OK;
+    }
+    GJ_CUDA_TRY(cudaMemcpyAsync(min_key, idx->d_col, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(max_key, idx->d_col + idx->n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    return GJ_OK;
+}
+
+uint32_t default_radix_bits(uint64_t n) {
+    // ~64K index keys (512 KB) per partition, fanout within [2^8, 2^12]
+    uint32_t b = 8;
+    while (b < kMaxRadixBits && (n >> b) > (1ull << 16)) ++b;
+    return b;
+}
+
+uint32_t shift_for(uint64_t min_key, uint64_t max_key, uint32_t radix_bits) {
+    const uint64_t range = max_key - min_key;
+    const unsigned used = range ? 64u - (unsigned)__builtin_clzll(range) : 0u;
+    return used > radix_bits ? used - radix_bits : 0u;
+}
+
+}  // namespace
+}  // namespace gj
+
+using namespace gj;
+
+extern "C" {
+
+int gj_partition_workspace_size(uint64_t m, uint32_t radix_bits, size_t* bytes) {
+    GJ_CHECK_ARG(bytes, "gj_partition_workspace_size: null argument");
+    GJ_CHECK_ARG(radix_bits >= 1 && radix_bits <= kMaxRadixBits, "gj_partition_workspace_size: radix_bits not in [1, 12]");
+    device_info di;
+    GJ_TRY(current_device_info(&di));
+    *bytes = partition_ws_bytes(m, radix_bits, di.sm_count);
+    return GJ_OK;
+}
+
+int gj_range_partition(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift, uint32_t radix_bits,
+                       uint64_t* d_out_keys, uint32_t* d_out_rows, uint64_t* d_offsets, void* d_workspace,
+                       size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(radix_bits >= 1 && radix_bits <= kMaxRadixBits, "gj_range_partition: radix_bits not in [1, 12]");
+    GJ_CHECK_ARG(m == 0 || (d_keys && d_out_keys && d_out_rows), "gj_range_partition: null buffer");
+    GJ_CHECK_ARG(shift < 64, "gj_range_partition: shift must be < 64");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_range_partition: row ids must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    return range_partition_impl(d_keys, m, min_key, shift, radix_bits, 0, d_out_keys, d_out_rows, d_offsets,
+                                d_workspace, workspace_bytes, as_stream(stream));
+}
+
+int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, const uint32_t* d_part_rows, uint64_t m,
+                          uint32_t* d_positions, void* stream) {
+    GJ_CHECK_ARG(index, "gj_partitioned_lookup: null index");
+    GJ_CHECK_ARG(m == 0 || (d_part_keys && d_part_rows && d_positions), "gj_partitioned_lookup: null buffer");
+    return launch_scatter_lookup(index, d_part_keys, d_part_rows, m, d_positions, as_stream(stream));
+}
+
+static uint64_t clamp_window(uint64_t m, uint64_t window) {
+    if (window == 0 || window > m) window = m;
+    return window ? window : 1;
+}
+
+int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
+                                       size_t* bytes) {
+    GJ_CHECK_ARG(index && bytes, "gj_partitioned_inlj_workspace_size: null argument");
+    GJ_CHECK_ARG(window_size > 0, "gj_partitioned_inlj_workspace_size: window_size must be > 0");
+    if (radix_bits == 0) radix_bits = default_radix_bits(index->n);
+    GJ_CHECK_ARG(radix_bits <= kMaxRadixBits, "gj_partitioned_inlj_workspace_size: radix_bits > 12");
+    device_info di;
+    GJ_TRY(current_device_info(&di));
+    const uint64_t w = window_size;
+    *bytes = workspace_carver::need({w * sizeof(uint64_t), w * sizeof(uint32_t),
+                                     partition_ws_bytes(w, radix_bits, di.sm_count), pairs_workspace_bytes(w)});
+    return GJ_OK;
+}
+
+int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint64_t window_size,
+                        uint32_t radix_bits, uint32_t* d_positions, uint32_t* d_pairs, uint64_t* d_count,
+                        void* d_workspace, size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(index, "gj_partitioned_inlj: null index");
+    GJ_CHECK_ARG(d_positions || d_pairs, "gj_partitioned_inlj: no output requested");
+    GJ_CHECK_ARG(!d_pairs || d_count, "gj_partitioned_inlj: d_count is required with d_pairs");
+    GJ_CHECK_ARG(m == 0 || d_probes, "gj_partitioned_inlj: null probes");
+    GJ_CHECK_ARG(window_size > 0, "gj_partitioned_inlj: window_size must be > 0");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_partitioned_inlj: probe rows must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    if (radix_bits == 0) radix_bits = default_radix_bits(index->n);
+    GJ_CHECK_ARG(radix_bits <= kMaxRadixBits, "gj_partitioned_inlj: radix_bits > 12");
+    cudaStream_t s = as_stream(stream);
+    device_info di;
+    GJ_TRY(current_device_info(&di));
+    const uint64_t w = window_size;
+    workspace_carver wc(d_workspace, workspace_bytes);
+    uint64_t* pkeys = wc.take<uint64_t>(w);
+    uint32_t* prows = wc.take<uint32_t>(w);
+    const size_t pws_bytes = partition_ws_bytes(w, radix_bits, di.sm_count);
+    void* pws = wc.take<char>(pws_bytes);
+    const size_t qws_bytes = pairs_workspace_bytes(w);
+    void* qws = wc.take<char>(qws_bytes);
+    if (!pkeys || !prows || !pws || !qws) {
+        size_t need = 0;
+        gj_partitioned_inlj_workspace_size(index, window_size, radix_bits, &need);
+        set_error("gj_partitioned_inlj: workspace of %zu bytes is smaller than the %zu required", workspace_bytes, need);
+        return GJ_ERR_WORKSPACE;
+    }
+    if (d_pairs) GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
+    if (m == 0) return GJ_OK;
+    uint64_t min_key = 0, max_key = 0;
+    GJ_TRY(index_key_range(index, &min_key, &max_key, s));
+    const uint32_t shift = shift_for(min_key, max_key, radix_bits);
+    for (uint64_t off = 0; off < m; off += w) {
+        const uint64_t len = std::min<uint64_t>(w, m - off);
+        GJ_TRY(range_partition_impl(d_probes + off, len, min_key, shift, radix_bits, off, pkeys, prows, nullptr, pws,
+                                    pws_bytes, s));
+        if (d_positions) GJ_TRY(launch_scatter_lookup(index, pkeys, prows, len, d_positions, s));
+        if (d_pairs) GJ_TRY(launch_pairs(index, pkeys, len, prows, d_pairs, d_count, d_count, qws, qws_bytes, s));
+    }
+    return GJ_OK;
+}
+
+}  // extern "C"

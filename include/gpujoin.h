@@ -1,0 +1,210 @@
+/*
+ * gpujoin.h -- C ABI of the GB300 index-nested-loop-join (INLJ) probe engine.
+ *
+ * Plain C: pointers, sizes and status codes only.  Device pointers are
+ * marked d_*, host pointers h_*; a stream is passed as void* (a cudaStream_t,
+ * NULL = the legacy default stream).  Every call returns GJ_OK (0) or a
+ * GJ_ERR_* code; gj_last_error_string() describes the last failure of the
+ * calling thread.  Calls are asynchronous on the given stream unless noted.
+ *
+ * Ownership: the caller owns every input, output and workspace buffer; the
+ * library owns the memory of a gj_index (its search structure) and frees it
+ * in gj_index_free().  An index borrows the caller's device column (d_keys),
+ * which must stay alive and unchanged for the lifetime of the index
+ * (binary_search_index / radix_spline_index borrow it the same way,
+ * src/indexes.cuh:223,365).
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * josefschmeisser/gpujoin).
+ */
+#ifndef GPUJOIN_H
+#define GPUJOIN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GJ_ABI_VERSION 1u
+
+/* status codes */
+#define GJ_OK 0
+#define GJ_ERR_INVALID_ARGUMENT 1   /* null pointer, bad size, bad enum */
+#define GJ_ERR_CUDA 2               /* a CUDA runtime call failed */
+#define GJ_ERR_UNSUPPORTED 3        /* valid request this build cannot serve */
+#define GJ_ERR_OUT_OF_MEMORY 4      /* device or host allocation failed */
+#define GJ_ERR_TIMEOUT 5            /* a bounded device wait gave up */
+#define GJ_ERR_UNSORTED 6           /* build keys not strictly increasing */
+#define GJ_ERR_WORKSPACE 7          /* workspace missing or too small */
+#define GJ_ERR_TOO_LARGE 8          /* size exceeds a documented limit */
+
+/* not-found marker of every position output:
+ * numeric_limits<value_t>::max() (src/indexes.cuh:101,184,262,344) with the
+ * 32-bit tid_t of src/tpch/tpch_14_common.cuh:18 */
+#define GJ_INVALID_POS 0xFFFFFFFFu
+
+/* index kinds; the first five keep the order of index_type_enum
+ * (src/indexes.hpp:5) */
+typedef enum gj_index_type {
+    GJ_INDEX_BTREE = 0,
+    GJ_INDEX_HARMONIA = 1,
+    GJ_INDEX_BINARY_SEARCH = 2,
+    GJ_INDEX_RADIX_SPLINE = 3,
+    GJ_INDEX_NO_OP = 4,
+    GJ_INDEX_LEARNED = 5 /* not in the reference: trained position model */
+} gj_index_type;
+
+/* learned root models */
+#define GJ_LEARNED_ROOT_LINEAR 0u
+#define GJ_LEARNED_ROOT_MLP 1u
+
+/* Build parameters.  Call gj_index_params_default() first, then override.
+ * Replaces the compile-time IndexConfiguration / constants of the reference
+ * (src/indexes.cuh:88-91,169-174,329-334; src/index_lookup_config.hpp:18-37). */
+typedef struct gj_index_params {
+    uint32_t struct_size;       /* = sizeof(gj_index_params) */
+    uint32_t btree_node_keys;   /* keys per B+tree node: 16, 32 or 64 (default 64) */
+    uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */
+    uint32_t rs_max_error;      /* RadixSpline spline error (default 32) */
+    uint32_t bs_cache_keys;     /* binary search: sampled keys staged in shared memory (default 4096, 0 = off) */
+    uint32_t smem_cache_bytes;  /* B+tree / Harmonia: upper levels staged in shared memory (default 16384) */
+    uint32_t learned_leaves;    /* learned index: linear leaf models (default 16384) */
+    uint32_t learned_root;      /* GJ_LEARNED_ROOT_LINEAR or GJ_LEARNED_ROOT_MLP (default MLP) */
+    uint32_t learned_hidden;    /* MLP hidden width (default 32, max 32) */
+    uint32_t learned_steps;     /* root training steps (default 600) */
+    uint32_t learned_batch;     /* root training batch (default 8192) */
+    float learned_lr;           /* root learning rate (Adam, default 3e-3) */
+    uint64_t seed;              /* training / sampling seed */
+} gj_index_params;
+
+typedef struct gj_index gj_index; /* opaque */
+
+/* ---- library ------------------------------------------------------------ */
+uint32_t gj_abi_version(void);
+const char* gj_last_error_string(void);
+void gj_index_params_default(gj_index_params* params);
+
+/* parse_index_type (src/indexes.cpp:5-19): "btree", "harmonia",
+ * "binary_search", "radix_spline", "no_op" (+ "learned").  Unknown names
+ * return GJ_ERR_INVALID_ARGUMENT ("unknown index type", as the reference). */
+int gj_parse_index_type(const char* name, int* out_type);
+/* type_name<...>::value() (src/indexes.cuh:149-154 etc.) */
+const char* gj_index_type_name(int type);
+
+/* ---- index build / lookup ------------------------------------------------ */
+/* abstract_index::construct (src/indexes.cuh:36) + the per-index construct()
+ * overrides (:126,218,285,364).  d_keys: n strictly increasing uint64 keys
+ * on the device.  h_keys may be NULL (the builder copies what it needs).
+ * Errors: n == 0 or n >= 2^32-1 (GJ_ERR_TOO_LARGE, the reference's
+ * "'value_t' does not suffice"), Harmonia with n % 32 != 0
+ * (GJ_ERR_INVALID_ARGUMENT, src/harmonia.cuh:350-352), unsorted keys
+ * (GJ_ERR_UNSORTED).  Synchronous: returns when the index is usable. */
+int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uint64_t n,
+                   const gj_index_params* params, void* stream, gj_index** out_index);
+int gj_index_free(gj_index* index);
+/* abstract_index::memory_consumption (src/indexes.cuh:38) in bytes */
+uint64_t gj_index_memory_consumption(const gj_index* index);
+int gj_index_get_type(const gj_index* index, int* out_type);
+uint64_t gj_index_size(const gj_index* index);
+/* learned index: recorded maximum prediction error (positions) and mean
+ * search-window width over the build keys */
+int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* mean_window);
+
+/* Plain INLJ probe, lookup_kernel (src/index_lookup_common.cuh:217-245):
+ * d_positions[i] = device_index_t::cooperative_lookup(d_probes[i]) with the
+ * reference's per-index result semantics:
+ *   binary_search, radix_spline, learned: lower bound, GJ_INVALID_POS at n
+ *     (src/indexes.cuh:357-361, :205-215);
+ *   btree, harmonia: position of an equal key, else GJ_INVALID_POS
+ *     (src/btree.cuh:504-531, src/harmonia.cuh:740-786);
+ *   no_op: GJ_INVALID_POS (src/indexes.cuh:384-406). */
+int gj_index_lookup(const gj_index* index, const uint64_t* d_probes, uint64_t m,
+                    uint32_t* d_positions, void* stream);
+
+/* ---- join materialisation ------------------------------------------------ */
+/* ij_lookup_kernel (src/tpch/tpch_14_ij.cu:371-407): probe and emit one
+ * (probe row, build position) pair -- two uint32 at d_pairs[2k], [2k+1] --
+ * per probe with a result, in probe order (deterministic; the reference's
+ * order follows its atomics).  *d_count (device) receives the pair count.
+ * d_pairs must hold 2*m uint32.  Workspace: gj_inlj_pairs_workspace_size. */
+int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
+int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                  uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---- partitioned INLJ ---------------------------------------------------- */
+/* Range partition of the probe side, replacing gpu_contiguous_prefix_sum_int64
+ * + gpu_chunked_laswwc_radix_partition_int64_int64 as called from
+ * run_on_stream (src/index_lookup_partitioning.cu:300-359).  Partition of a
+ * key = min(((key - min_key) >> shift), 2^radix_bits - 1), keys <= min_key in
+ * partition 0.  Output is stable (probe order within a partition):
+ * d_out_keys / d_out_rows hold m entries, d_offsets 2^radix_bits + 1.
+ * radix_bits in [1, 12]. */
+int gj_partition_workspace_size(uint64_t m, uint32_t radix_bits, size_t* bytes);
+int gj_range_partition(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift,
+                       uint32_t radix_bits, uint64_t* d_out_keys, uint32_t* d_out_rows,
+                       uint64_t* d_offsets, void* d_workspace, size_t workspace_bytes, void* stream);
+/* partitioned_lookup_kernel (src/index_lookup_partitioning.cu:218-248):
+ * probe a partitioned relation and scatter d_positions[row] = result. */
+int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, const uint32_t* d_part_rows,
+                          uint64_t m, uint32_t* d_positions, void* stream);
+/* The windowed partitioned INLJ (partitioning_approach::run,
+ * src/index_lookup_partitioning.cu:436-507): the probe column is cut into
+ * windows of window_size probes; each window is range-partitioned on the
+ * index's key range and probed partition by partition.  Emits d_positions
+ * in probe order (equal to gj_index_lookup) when d_positions != NULL, and/or
+ * (row, pos) pairs of the matches in partition order when d_pairs != NULL
+ * (*d_count = number of pairs).  radix_bits = 0 picks the fanout from the
+ * index size.  Workspace: gj_partitioned_inlj_workspace_size. */
+int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
+                                       size_t* bytes);
+int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint64_t window_size,
+                        uint32_t radix_bits, uint32_t* d_positions, uint32_t* d_pairs, uint64_t* d_count,
+                        void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---- star-join aggregate -------------------------------------------------- */
+/* ij_plain_kernel (src/tpch/tpch_14_ij.cu:34-85) with the semantics of
+ * query_14_part_build (src/tpch/cpu_only.cpp:230-275): over fact rows with
+ * lo <= date < hi whose foreign key is found in the dimension index,
+ * summand = price * (100 - discount); d_out[1] += summand, and d_out[0] +=
+ * summand when d_dim_flag[dim position] != 0.  d_out (2 x int64, device) is
+ * overwritten.  dim_index must be an exact-match index (btree or harmonia). */
+int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk, const uint32_t* d_date,
+                     const int64_t* d_price, const int64_t* d_discount, uint64_t nfact,
+                     const uint8_t* d_dim_flag, uint32_t lo, uint32_t hi, int64_t* d_out, void* stream);
+
+/* ---- batched lookup stream ------------------------------------------------ */
+/* Many probe batches against several indexes (not in the reference).  Batch
+ * b probes d_probes[probe_offset[b] .. +batch_size[b]) against
+ * indexes[batch_index[b]] and writes d_positions at the same offsets.  The
+ * descriptor arrays are host arrays; mode 0 = one persistent kernel over all
+ * batches, mode 1 = one launch per batch (the baseline).  If
+ * d_batch_done_ns != NULL it receives, per batch, the device globaltimer
+ * (ns) when the batch's last probe finished. */
+int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32_t* h_batch_index,
+                    const uint64_t* h_probe_offset, const uint64_t* h_batch_size, uint32_t num_batches,
+                    const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
+                    uint64_t* d_batch_done_ns, void* d_workspace, size_t workspace_bytes, void* stream);
+int gj_batch_workspace_size(uint32_t num_indexes, uint32_t num_batches, size_t* bytes);
+
+/* ---- synthetic inputs (src/index_lookup_common.cuh:44-206, src/zipf.hpp) --- */
+/* n strictly increasing keys, iid-uniform in distribution over [0, upper)
+ * (sorted order statistics from exponential spacings).  Workspace:
+ * gj_generate_workspace_size. */
+int gj_generate_workspace_size(uint64_t n, size_t* bytes);
+int gj_generate_sorted_keys(uint64_t* d_keys, uint64_t n, uint32_t distribution, uint64_t upper,
+                            uint64_t seed, void* d_workspace, size_t workspace_bytes, void* stream);
+#define GJ_DIST_UNIFORM 0u
+#define GJ_DIST_LOGNORMAL 1u   /* lognormal(0, 2) scaled by 2^60, clipped to [0, upper) */
+#define GJ_DIST_CLUSTERS 2u    /* 1024 dense runs separated by random gaps */
+/* m probes d_probes[i] = d_keys[perm(rank_i - 1)], rank_i ~ Zipf(theta) over
+ * [1, n] (theta = 0: uniform), perm a seeded permutation of [0, n).
+ * absent_fraction of the probes are replaced by keys not in the column. */
+int gj_generate_probes(const uint64_t* d_keys, uint64_t n, uint64_t* d_probes, uint64_t m, double theta,
+                       double absent_fraction, uint64_t seed, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUJOIN_H */

@@ -1,0 +1,85 @@
+"""The C ABI surface of libgpujoin.so, checked without a GPU: the library
+loads, exports every function include/gpujoin.h declares, and rejects bad
+arguments before touching the device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gpujoin.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gj_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "gj_index_build" in names and "gj_index_lookup" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol(gj):
+    L = gj.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, f"symbols declared in gpujoin.h but not exported: {missing}"
+
+
+def test_bindings_cover_header(gj):
+    assert sorted(gj.exported_symbols()) == declared_functions()
+
+
+def test_abi_version_and_names(gj):
+    L = gj.lib()
+    assert L.gj_abi_version() == 1
+    for t in gj.index_type_enum:
+        assert L.gj_index_type_name(int(t)).decode() == t.name
+    assert L.gj_index_type_name(99) is None
+
+
+def test_parse_index_type(gj):
+    # src/indexes.cpp:5-19
+    for name in ("btree", "harmonia", "binary_search", "radix_spline", "no_op", "learned"):
+        assert gj.parse_index_type(name).name == name
+    with pytest.raises(RuntimeError, match="unknown index type"):
+        gj.parse_index_type("hash_table")
+
+
+def test_params_defaults(gj):
+    p = gj.default_params()
+    assert p.struct_size == ctypes.sizeof(gj.gj_index_params)
+    assert p.btree_node_keys == 64 and p.rs_radix_bits == 18 and p.rs_max_error == 32
+    assert p.learned_leaves == 16384 and p.learned_hidden == 32
+
+
+def test_argument_errors_without_device(gj):
+    L = gj.lib()
+    out = ctypes.c_void_p()
+    assert L.gj_index_build(0, None, None, 10, None, None, None) == 1
+    assert L.gj_index_build(42, None, None, 10, None, None, ctypes.byref(out)) == 1
+    assert b"unknown index type" in L.gj_last_error_string()
+    assert L.gj_index_lookup(None, None, 0, None, None) == 1
+    assert L.gj_index_free(None) == 0
+    sz = ctypes.c_size_t()
+    assert L.gj_inlj_pairs_workspace_size(1 << 20, ctypes.byref(sz)) == 0 and sz.value > 0
+    assert L.gj_partition_workspace_size(100, 0, ctypes.byref(sz)) == 1
+    assert L.gj_partition_workspace_size(100, 13, ctypes.byref(sz)) == 1
+    assert L.gj_generate_workspace_size(1000, ctypes.byref(sz)) == 0
+
+
+def test_oversized_column_rejected(gj):
+    L = gj.lib()
+    out = ctypes.c_void_p()
+    # 2^32 - 1 keys cannot be addressed by 32-bit positions ('value_t' does not suffice)
+    assert L.gj_index_build(2, ctypes.c_void_p(16), None, (1 << 32) - 1, None, None, ctypes.byref(out)) == 8
+
+
+def test_experiment_config_defaults(gj):
+    # src/index_lookup_config.hpp:18-37
+    c = gj.experiment_config()
+    assert c.approach == "plain" and c.index_type == "btree" and c.block_size == 128
+    assert c.partitioning_approach_window_size == 10000 and gj.radix_bits == 11

@@ -1,0 +1,137 @@
+"""Join materialisation, partitioned INLJ and the star-join aggregate on the
+GPU against the CPU oracle."""
+import numpy as np
+import pytest
+
+from test_lookup_gpu import column, expected, from_dev_u32, probes_for, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def pairs_of(out_pairs, count):
+    c = int(count.item())
+    a = out_pairs[: 2 * c].cpu().numpy().view(np.uint32).reshape(-1, 2)
+    return a[:, 0].copy(), a[:, 1].copy()
+
+
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline"])
+@pytest.mark.parametrize("m", [0, 1, 31, 2047, 2048, 2049, 100003])
+def test_inlj_pairs_match_oracle(orc, gj, cuda, kind, m):
+    import torch
+
+    rng = np.random.default_rng(m + 3)
+    col = column(rng, 32 * 1000)
+    pr = probes_for(rng, col, max(m, 1))[:m]
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    out, cnt = ix.inlj_pairs(to_dev(torch, pr) if m else torch.empty(0, dtype=torch.int64, device="cuda"))
+    rows, pos = pairs_of(out, cnt)
+    erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
+    np.testing.assert_array_equal(rows, erows)
+    np.testing.assert_array_equal(pos, epos)
+
+
+def test_inlj_pairs_all_absent(orc, gj, cuda):
+    import torch
+
+    col = np.arange(0, 3200, dtype=np.uint64) * 2
+    pr = np.arange(1, 6401, 2, dtype=np.uint64)  # odd keys: none present
+    ix = gj.btree_index().construct(None, to_dev(torch, col))
+    out, cnt = ix.inlj_pairs(to_dev(torch, pr))
+    assert int(cnt.item()) == 0
+
+
+@pytest.mark.parametrize("bits", [1, 4, 8, 12])
+def test_range_partition_matches_oracle(orc, gj, cuda, bits):
+    import torch
+
+    rng = np.random.default_rng(bits)
+    keys = rng.integers(0, 1 << 48, 300001, dtype=np.uint64)
+    min_key, shift = 1 << 20, 48 - bits
+    rel = gj.range_partition(to_dev(torch, keys), min_key, shift, bits)
+    ok, orows, offs = orc.range_partition(keys, min_key, shift, bits)
+    np.testing.assert_array_equal(rel.offsets.cpu().numpy().view(np.uint64), offs)
+    gk = rel.keys.cpu().numpy().view(np.uint64)
+    gr = rel.rows.cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(keys[gr], gk)
+    # same tuples per partition (the order inside a partition is not fixed)
+    for p in range(1 << bits):
+        a, b = int(offs[p]), int(offs[p + 1])
+        np.testing.assert_array_equal(np.sort(gr[a:b]), np.sort(orows[a:b]))
+
+
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline"])
+@pytest.mark.parametrize("window", [0, 1000, 65536])
+def test_partitioned_inlj_equals_plain(orc, gj, cuda, kind, window):
+    import torch
+
+    rng = np.random.default_rng(window + 17)
+    col = column(rng, 32 * 5000)
+    pr = probes_for(rng, col, 120000)
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=0, positions=True,
+                                        pairs=True)
+    exp = expected(orc, kind, col, pr)
+    np.testing.assert_array_equal(from_dev_u32(pos), exp)
+    rows, bpos = pairs_of(prs, cnt)
+    erows, epos = orc.pairs_from_positions(exp)
+    order = np.argsort(rows, kind="stable")
+    np.testing.assert_array_equal(rows[order], erows)
+    np.testing.assert_array_equal(bpos[order], epos)
+
+
+@pytest.mark.parametrize("bits", [8, 10, 12])
+def test_partitioned_inlj_fanouts(orc, gj, cuda, bits):
+    import torch
+
+    rng = np.random.default_rng(bits + 50)
+    col = column(rng, 1 << 18)
+    pr = probes_for(rng, col, 200000)
+    ix = gj.btree_index().construct(None, to_dev(torch, col))
+    pos, _, _ = ix.partitioned_inlj(to_dev(torch, pr), radix_bits=bits)
+    np.testing.assert_array_equal(from_dev_u32(pos), orc.exact_lookup(col, pr))
+
+
+def star_inputs(rng, nfact, ndim):
+    dim = np.arange(1, ndim + 1, dtype=np.uint64)
+    flag = np.zeros(ndim, dtype=np.uint8)
+    flag[rng.choice(ndim, ndim // 6, replace=False)] = 1
+    fk = rng.integers(1, ndim + 1, nfact).astype(np.uint32)
+    fk[rng.integers(0, nfact, nfact // 50)] = ndim + 7  # dangling foreign keys
+    date = rng.integers(0, 2556, nfact).astype(np.uint32)
+    price = rng.integers(90000, 10500001, nfact).astype(np.int64)
+    disc = rng.integers(0, 11, nfact).astype(np.int64)
+    return dim, flag, fk, date, price, disc
+
+
+@pytest.mark.parametrize("kind", ["btree", "harmonia", "binary_search", "radix_spline"])
+@pytest.mark.parametrize("nfact", [0, 1, 4095, 4097, 600000])
+def test_star_join_matches_oracle(orc, gj, cuda, kind, nfact):
+    import torch
+
+    rng = np.random.default_rng(nfact + 1)
+    ndim = 20000
+    dim, flag, fk, date, price, disc = star_inputs(rng, max(nfact, 1), ndim)
+    fk, date, price, disc = fk[:nfact], date[:nfact], price[:nfact], disc[:nfact]
+    lo, hi = 1000, 1030
+    ix = gj.make_index(kind).construct(None, to_dev(torch, dim))
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()
+    out = gj.star_join_sum(ix, t(fk.view(np.int32), torch.int32), t(date.view(np.int32), torch.int32),
+                           t(price, torch.int64), t(disc, torch.int64), t(flag, torch.uint8), lo, hi)
+    num, den = orc.star_join(fk, date, price, disc, dim, flag, lo, hi)
+    got = out.cpu().numpy()
+    assert int(got[0]) == num and int(got[1]) == den
+
+
+def test_star_join_full_window_and_empty_window(orc, gj, cuda):
+    import torch
+
+    rng = np.random.default_rng(99)
+    dim, flag, fk, date, price, disc = star_inputs(rng, 100000, 5000)
+    ix = gj.btree_index().construct(None, to_dev(torch, dim))
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()
+    args = (t(fk.view(np.int32), torch.int32), t(date.view(np.int32), torch.int32), t(price, torch.int64),
+            t(disc, torch.int64), t(flag, torch.uint8))
+    for lo, hi in ((0, 1 << 31), (500, 500), (2555, 2556)):
+        got = gj.star_join_sum(ix, *args, lo, hi).cpu().numpy()
+        num, den = orc.star_join(fk, date, price, disc, dim, flag, lo, hi)
+        assert (int(got[0]), int(got[1])) == (num, den)

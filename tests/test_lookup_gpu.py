@@ -1,0 +1,200 @@
+"""Parity of the CUDA probe kernels (through the C ABI) against the CPU oracle.
+
+Bit-exact: every position must equal the oracle's restatement of the
+reference lookup for the index kind."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LOWER_BOUND_KINDS = ("binary_search", "radix_spline")
+EXACT_KINDS = ("btree", "harmonia")
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).cuda()
+
+
+def from_dev_u32(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+def column(rng, n, upper=1 << 63):
+    while True:
+        k = np.unique(rng.integers(0, upper, size=n + n // 4 + 16, dtype=np.uint64))
+        if len(k) >= n:
+            return np.sort(rng.choice(k, size=n, replace=False))
+
+
+def probes_for(rng, col, m):
+    n = len(col)
+    parts = [col[rng.integers(0, n, size=m)], rng.integers(0, 1 << 63, size=m // 3 + 1, dtype=np.uint64),
+             np.array([0, col[0], col[-1], col[-1] + 1, (1 << 64) - 1, 1 << 63], dtype=np.uint64),
+             col[:8], col[-8:], col[rng.integers(0, n, size=8)].repeat(4)]
+    if col[0] > 0:
+        parts.append(np.array([col[0] - 1], dtype=np.uint64))
+    return np.concatenate(parts).astype(np.uint64)
+
+
+def expected(orc, kind, col, pr):
+    if kind in LOWER_BOUND_KINDS or kind == "learned":
+        return orc.bs_lookup(col, pr)
+    if kind == "no_op":
+        return np.full(len(pr), 0xFFFFFFFF, dtype=np.uint32)
+    return orc.exact_lookup(col, pr)
+
+
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline"])
+@pytest.mark.parametrize("n", [32, 64, 96, 2048, 32 * 1090, 100000 - 100000 % 32, 1 << 20])
+def test_lookup_matches_oracle(orc, gj, cuda, kind, n):
+    import torch
+
+    rng = np.random.default_rng(n * 7 + len(kind))
+    col = column(rng, n)
+    pr = probes_for(rng, col, 5000)
+    d_col, d_pr = to_dev(torch, col), to_dev(torch, pr)
+    ix = gj.make_index(kind).construct(col, d_col)
+    got = from_dev_u32(ix.lookup(d_pr))
+    exp = expected(orc, kind, col, pr)
+    bad = np.nonzero(got != exp)[0]
+    assert len(bad) == 0, f"{kind} n={n}: {len(bad)} mismatches, first {bad[:5]} got {got[bad[:5]]} exp {exp[bad[:5]]}"
+
+
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "radix_spline"])
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 63, 65, 4095, 4097])
+def test_lookup_small_ragged_sizes(orc, gj, cuda, kind, n):
+    import torch
+
+    rng = np.random.default_rng(n + 100)
+    col = column(rng, n, upper=1 << 20)
+    pr = np.concatenate([np.arange(0, (1 << 20) + 10, 997, dtype=np.uint64), col])
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+    np.testing.assert_array_equal(got, expected(orc, kind, col, pr))
+
+
+@pytest.mark.parametrize("node_keys", [16, 32, 64])
+def test_btree_node_widths(orc, gj, cuda, node_keys):
+    import torch
+
+    rng = np.random.default_rng(node_keys)
+    for n in (1, node_keys - 1, node_keys, node_keys + 1, node_keys ** 2 + 3, 123457):
+        col = column(rng, n)
+        pr = probes_for(rng, col, 3000)
+        ix = gj.btree_index(btree_node_keys=node_keys).construct(None, to_dev(torch, col))
+        got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"W={node_keys} n={n}")
+
+
+@pytest.mark.parametrize("cache_keys", [0, 2, 64, 4096])
+def test_binary_search_cache_settings(orc, gj, cuda, cache_keys):
+    import torch
+
+    rng = np.random.default_rng(cache_keys + 1)
+    for n in (100, 5000, 300001):
+        col = column(rng, n)
+        pr = probes_for(rng, col, 4000)
+        ix = gj.binary_search_index(bs_cache_keys=cache_keys).construct(None, to_dev(torch, col))
+        np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), orc.bs_lookup(col, pr))
+
+
+@pytest.mark.parametrize("bits,err", [(18, 32), (8, 4), (20, 0), (2, 64)])
+def test_radix_spline_parameters(orc, gj, cuda, bits, err):
+    import torch
+
+    rng = np.random.default_rng(bits * 100 + err)
+    col = column(rng, 200000)
+    pr = probes_for(rng, col, 20000)
+    ix = gj.radix_spline_index(rs_radix_bits=bits, rs_max_error=err).construct(None, to_dev(torch, col))
+    np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), orc.bs_lookup(col, pr))
+
+
+def test_harmonia_golden_fixture(orc, gj, cuda):
+    import os
+
+    import torch
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "harmonia.npz"))
+    sizes = sorted({int(k.split("_")[1]) for k in d.files})
+    for n in sizes:
+        col, pr = d[f"harmonia_{n}_col"], d[f"harmonia_{n}_probes"]
+        ix = gj.harmonia_index().construct(None, to_dev(torch, col))
+        np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), d[f"harmonia_{n}_pos"],
+                                      err_msg=f"n={n}")
+
+
+def test_btree_golden_fixture(orc, gj, cuda):
+    import os
+
+    import torch
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "btree.npz"))
+    sizes = sorted({int(k.split("_")[1]) for k in d.files})
+    for n in sizes:
+        col, pr = d[f"btree_{n}_col"], d[f"btree_{n}_probes"]
+        ix = gj.btree_index().construct(None, to_dev(torch, col))
+        np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), d[f"btree_{n}_pos"],
+                                      err_msg=f"n={n}")
+
+
+def test_no_op_index(gj, cuda):
+    import torch
+
+    ix = gj.no_op_index().construct(None, torch.zeros(4, dtype=torch.int64, device="cuda"))
+    got = from_dev_u32(ix.lookup(torch.arange(100, dtype=torch.int64, device="cuda")))
+    assert np.all(got == 0xFFFFFFFF)
+
+
+def test_empty_probe_column(gj, cuda):
+    import torch
+
+    col = torch.arange(0, 64, dtype=torch.int64, device="cuda") * 3
+    for kind in ("binary_search", "btree", "harmonia", "radix_spline"):
+        ix = gj.make_index(kind).construct(None, col)
+        out = ix.lookup(torch.empty(0, dtype=torch.int64, device="cuda"))
+        assert out.numel() == 0
+
+
+def test_build_errors(gj, cuda):
+    import torch
+
+    unsorted = torch.tensor([5, 3, 9, 10], dtype=torch.int64, device="cuda")
+    with pytest.raises(gj.GJError) as e:
+        gj.btree_index().construct(None, unsorted)
+    assert e.value.code == 6
+    dup = torch.tensor([1, 2, 2, 3], dtype=torch.int64, device="cuda")
+    with pytest.raises(gj.GJError):
+        gj.binary_search_index().construct(None, dup)
+    not32 = torch.arange(0, 33, dtype=torch.int64, device="cuda")
+    with pytest.raises(gj.GJError) as e:
+        gj.harmonia_index().construct(None, not32)
+    assert e.value.code == 1
+    with pytest.raises(gj.GJError):
+        gj.btree_index(btree_node_keys=48).construct(None, torch.arange(0, 100, dtype=torch.int64, device="cuda"))
+    with pytest.raises(gj.GJError):
+        gj.btree_index().construct(None, torch.empty(0, dtype=torch.int64, device="cuda"))
+
+
+def test_memory_consumption(gj, cuda):
+    import torch
+
+    col = torch.arange(0, 1 << 16, dtype=torch.int64, device="cuda") * 5
+    assert gj.binary_search_index(bs_cache_keys=0).construct(None, col).memory_consumption() == 0
+    assert gj.btree_index().construct(None, col).memory_consumption() > 0
+    assert gj.harmonia_index().construct(None, col).memory_consumption() > 0
+    assert gj.radix_spline_index().construct(None, col).memory_consumption() > 0
+
+
+def test_lookup_on_side_stream(orc, gj, cuda):
+    import torch
+
+    rng = np.random.default_rng(77)
+    col = column(rng, 50000)
+    pr = probes_for(rng, col, 50000)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        d_col, d_pr = to_dev(torch, col), to_dev(torch, pr)
+        ix = gj.btree_index().construct(None, d_col, stream=s)
+        out = ix.lookup(d_pr, stream=s)
+    s.synchronize()
+    np.testing.assert_array_equal(from_dev_u32(out), orc.exact_lookup(col, pr))
