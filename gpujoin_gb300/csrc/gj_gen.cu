@@ -181,7 +181,7 @@ __global__ void k_total(const uint64_t* __restrict__ d, uint64_t n, uint64_t* __
 }
 
 // key_i = floor(S_i * upper / T), exact in 128 bits (strictly increasing
-// because every gap >= 2 and upper / T > 1/2)
+// because every gap >= 2 and upper / T > 1)
 __global__ void k_scale(uint64_t* __restrict__ d, uint64_t n, uint64_t upper, const uint64_t* __restrict__ aux) {
     const uint64_t T = aux[1];
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -399,7 +399,10 @@ int gj_generate_sorted_keys(uint64_t* d_keys, uint64_t n, uint32_t distribution,
 
     // sorted uniform order statistics in [0, U): exponential spacings
     const uint64_t U = distribution == GJ_DIST_UNIFORM ? upper : (1ull << 53);
-    const double mean = (double)U / (double)(n + 1);
+    // spacings are drawn at 1/64 of their final scale: an Exp(1) variate from a
+    // 53-bit uniform is at most 36.8, so the n+1 spacings sum to at most
+    // 0.58 * U < 2^63 and never overflow; the rescale below multiplies by > 1
+    const double mean = (double)U / (double)(n + 1) / 64.0;
     k_gaps<<<grid, 256, 0, s>>>(d_keys, n, mean, seed);
     k_gaps<<<1, 32, 0, s>>>(aux, 1, mean, mix64(seed ^ 0x7a11ull));  // the (n+1)-th spacing
     GJ_TRY(inclusive_scan_sum(d_keys, n, scan_ws, scan_bytes, s));

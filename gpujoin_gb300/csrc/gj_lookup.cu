@@ -139,8 +139,9 @@ __global__ void __launch_bounds__(kBlock) k_pairs(const Op op, const stage_desc 
                                                   uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
                                                   uint64_t* __restrict__ d_count, pairs_ws ws, uint32_t num_tiles) {
     extern __shared__ uint64_t cache[];
+    constexpr int kWarps = kBlock / 32;
     __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_warp[kBlock / 32];
+    __shared__ uint32_t s_cnt[kItems * kWarps];
     __shared__ unsigned long long s_prefix;
     __shared__ int s_abort;
     stage_cache(cache, sd);
@@ -157,38 +158,48 @@ __global__ void __launch_bounds__(kBlock) k_pairs(const Op op, const stage_desc 
         if (tile >= num_tiles) break;
         const uint64_t t0 = (uint64_t)tile * kTile;
 
+        // item k of thread t is probe t0 + k * kBlock + t: coalesced loads;
+        // output order is probe order, i.e. (k, warp, lane) order
         uint32_t pos[kItems];
-        uint32_t mine = 0;
+        uint32_t lane_rank[kItems];
+        uint32_t flags = 0;
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
             pos[k] = kInvalid;
-            if (i < m) {
-                pos[k] = op(cache, __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)));
-                mine += (pos[k] != kInvalid);
-            }
+            if (i < m) pos[k] = op(cache, __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)));
+            const bool hit = pos[k] != kInvalid;
+            const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
+            lane_rank[k] = __popc(ballot & ((1u << lane) - 1u));
+            if (hit) flags |= 1u << k;
+            if (lane == 0) s_cnt[k * kWarps + warp] = __popc(ballot);
         }
-        // block-wide exclusive scan of the per-thread match counts
-        uint32_t incl = mine;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= (uint32_t)d) incl += t;
-        }
-        if (lane == 31) s_warp[warp] = incl;
         __syncthreads();
         if (warp == 0) {
-            uint32_t w = lane < kBlock / 32 ? s_warp[lane] : 0u;
-            uint32_t wi = w;
+            // exclusive scan of the kItems * kWarps counts in (k, warp) order
+            constexpr int kPerLane = kItems * kWarps / 32;
+            uint32_t v[kPerLane];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) {
+                v[j] = s_cnt[lane * kPerLane + j];
+                sum += v[j];
+            }
+            uint32_t incl = sum;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, wi, d);
-                if (lane >= (uint32_t)d) wi += t;
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (uint32_t)d) incl += t;
             }
-            if (lane < kBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-            if (lane == kBlock / 32 - 1) {
+            uint32_t run = incl - sum;
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) {
+                s_cnt[lane * kPerLane + j] = run;
+                run += v[j];
+            }
+            if (lane == 31) {
                 // publish the tile aggregate, then resolve the tile prefix
-                const unsigned long long total = wi;
+                const unsigned long long total = incl;
                 unsigned long long prefix = 0;
                 if (tile == 0) {
                     atomicExch(&ws.tile_state[0], kFlagPrefix | total);
@@ -219,14 +230,14 @@ __global__ void __launch_bounds__(kBlock) k_pairs(const Op op, const stage_desc 
         }
         __syncthreads();
         if (s_abort) break;
-        uint64_t o = base + s_prefix + s_warp[warp] + (incl - mine);
+        const uint64_t tile_base = base + s_prefix;
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            if (i < m && pos[k] != kInvalid) {
+            if (flags & (1u << k)) {
+                const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+                const uint64_t o = tile_base + s_cnt[k * kWarps + warp] + lane_rank[k];
                 const uint32_t row = rows ? __ldcs(rows + i) : (uint32_t)i;
                 __stcs(reinterpret_cast<unsigned long long*>(pairs + o), ((unsigned long long)pos[k] << 32) | row);
-                ++o;
             }
         }
         __syncthreads();
