@@ -384,7 +384,7 @@ def parse_args(argv=None):
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)
     ap.add_argument("--theta", type=float, default=0.5)
-    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search")
+    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
     ap.add_argument("--no-cpu-baseline", action="store_true")

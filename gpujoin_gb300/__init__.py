@@ -20,7 +20,7 @@ import os
 from typing import Optional, Tuple
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgpujoin.so")
+LIB_PATH = os.environ.get("GJ_LIB_PATH", os.path.join(HERE, "libgpujoin.so"))
 
 INVALID_POS = 0xFFFFFFFF
 
@@ -109,6 +109,7 @@ _SIGNATURES = {
     "gj_partitioned_inlj_workspace_size": (_i32, [_vp, _u64, _u32, ctypes.POINTER(_sz)]),
     "gj_partitioned_inlj": (_i32, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_star_join_sum": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
+    "gj_learned_mlp_grad": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_batch_lookup": (_i32, [ctypes.POINTER(_vp), _u32, _vp, _vp, _vp, _u32, _vp, _vp, _u32, _vp, _vp, _sz, _vp]),
     "gj_batch_workspace_size": (_i32, [_u32, _u32, ctypes.POINTER(_sz)]),
     "gj_generate_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
@@ -425,6 +426,17 @@ def star_join_sum(dim_index: abstract_index, d_fk, d_date, d_price, d_discount, 
     _check(lib().gj_star_join_sum(dim_index.handle, _ptr(d_fk), _ptr(d_date), _ptr(d_price), _ptr(d_discount),
                                   d_fk.numel(), _ptr(d_dim_flag), lo, hi, _ptr(out), _stream(stream)))
     return out
+
+
+def learned_mlp_grad(d_params, hidden: int, d_x, d_y, stream=None):
+    """GPU backward pass of the learned root MLP: (gradient of the summed
+    squared error, that sum) over the samples (x, y)."""
+    torch = _torch()
+    grad = torch.empty_like(d_params)
+    loss = torch.zeros(1, dtype=torch.float64, device=d_params.device)
+    _check(lib().gj_learned_mlp_grad(_ptr(d_params), hidden, _ptr(d_x), _ptr(d_y), d_x.numel(), _ptr(grad),
+                                     _ptr(loss), _stream(stream)))
+    return grad, loss
 
 
 # --------------------------------------------------------------------------

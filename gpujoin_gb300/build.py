@@ -16,8 +16,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(HERE, "libgpujoin.so")
+BUILD = os.environ.get("GJ_BUILD_DIR", os.path.join(HERE, "_build"))
+LIB = os.environ.get("GJ_LIB_PATH", os.path.join(HERE, "libgpujoin.so"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

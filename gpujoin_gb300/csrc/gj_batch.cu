@@ -182,7 +182,7 @@ int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32
         switch (ix->type) {
             case GJ_INDEX_BINARY_SEARCH: v.u.bs = ix->bs; break;
             case GJ_INDEX_BTREE: v.u.bt = ix->bt; v.u.bt.cached_levels = 0; break;
-            case GJ_INDEX_HARMONIA: v.u.hm = ix->hm; v.u.hm.cached_nodes = 0; break;
+            case GJ_INDEX_HARMONIA: v.u.hm = ix->hm; v.u.hm.cached_nodes = 0; v.u.hm.cached_levels = 0; break;
             case GJ_INDEX_RADIX_SPLINE: v.u.rs = ix->rs; break;
             case GJ_INDEX_LEARNED: v.u.ln = ix->ln; break;
             default: break;

@@ -57,6 +57,8 @@ int build_harmonia_arrays(const uint64_t* col, uint64_t n, harmonia_arrays* out)
     const uint64_t inner_size = K * leaf.node_prefix;
 
     out->depth = depth;
+    out->level_nodes.clear();
+    for (const auto& l : levels) out->level_nodes.push_back(l.node_count);
     out->keys.assign(inner_size, UINT64_MAX);
     out->children.assign(total_nodes, 0);
 

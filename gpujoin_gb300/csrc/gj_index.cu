@@ -238,11 +238,17 @@ int build_harmonia(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
     idx->hm.n = idx->n;
     idx->hm.inner_size = ha.keys.size();
     idx->hm.depth = ha.depth;
-    const uint64_t inner_nodes = ha.keys.size() / kHarmoniaKeys;
+    // shared-memory cache: whole top levels (keys + children) within the budget
     const uint64_t per_node = (kHarmoniaKeys + 1) * sizeof(uint64_t);
-    uint64_t cached = idx->params.smem_cache_bytes / per_node;
-    if (cached > inner_nodes) cached = inner_nodes;
+    uint64_t cached = 0;
+    uint32_t cached_levels = 0;
+    for (uint32_t l = 0; l + 1 < ha.depth; ++l) {
+        if ((cached + ha.level_nodes[l]) * per_node > idx->params.smem_cache_bytes) break;
+        cached += ha.level_nodes[l];
+        cached_levels += 1;
+    }
     idx->hm.cached_nodes = (uint32_t)cached;
+    idx->hm.cached_levels = cached_levels;
     idx->bytes = (ha.keys.size() + ha.children.size()) * sizeof(uint64_t);
     return GJ_OK;
 }
@@ -277,6 +283,9 @@ int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t
 }  // namespace
 
 int build_learned(gj_index* idx, cudaStream_t s);  // gj_learned.cu
+
+// owned allocation of an index (released by gj_index_free)
+int device_alloc_for(gj_index* idx, size_t bytes, void** out) { return device_alloc(idx, bytes, out); }
 
 }  // namespace gj
 

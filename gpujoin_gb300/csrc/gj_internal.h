@@ -78,6 +78,7 @@ struct workspace_carver {
 struct harmonia_arrays {
     std::vector<uint64_t> keys;      // inner key array, 32 per inner node
     std::vector<uint64_t> children;  // per node
+    std::vector<uint64_t> level_nodes;  // nodes per level, root first
     uint32_t depth = 0;
 };
 // returns GJ_OK or an error code (n % 32 != 0, depth limit)

@@ -183,6 +183,7 @@ extern "C" int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk,
     bt.cached_levels = 0;
     harmonia_view hm = idx->hm;
     hm.cached_nodes = 0;
+    hm.cached_levels = 0;
     switch (idx->type) {
         case GJ_INDEX_BTREE:
             if (idx->bt_logw == 4) return run_star_join(join_btree4{bt}, idx, d_fk, d_date, d_price, d_discount, nfact, d_dim_flag, lo, hi, d_out, s);

@@ -20,6 +20,10 @@ namespace gj {
 namespace {
 
 constexpr int kBlock = 256;
+// resident blocks per SM the lookup kernels are compiled for (register cap)
+#ifndef GJ_MIN_BLOCKS
+#define GJ_MIN_BLOCKS 1
+#endif
 
 // ---------------------------------------------------------------------------
 // per-index lookup functors
@@ -36,6 +40,10 @@ struct op_bs {
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return bs_lookup(v, cache, key);
     }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
+        bs_lookup_batch<K>(v, cache, key, res);
+    }
 };
 template <int LOGW>
 struct op_btree {
@@ -43,24 +51,45 @@ struct op_btree {
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return btree_lookup<LOGW>(v, cache, key);
     }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
+        btree_lookup_batch<LOGW, K>(v, cache, key, res);
+    }
 };
 struct op_harmonia {
     harmonia_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return harmonia_lookup(v, cache, key);
     }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
+        harmonia_lookup_batch<K>(v, cache, key, res);
+    }
 };
 struct op_rs {
     rs_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const { return rs_lookup(v, key); }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t*, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
+        rs_lookup_batch<K>(v, key, res);
+    }
 };
 struct op_noop {
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t*, const uint64_t (&)[K], uint32_t (&res)[K]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k) res[k] = kInvalid;
+    }
 };
 struct op_learned {
     learned_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return learned_lookup(v, reinterpret_cast<const float*>(cache), key);
+    }
+    template <int K>
+    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
+        learned_lookup_batch<K>(v, reinterpret_cast<const float*>(cache), key, res);
     }
 };
 
@@ -74,42 +103,61 @@ __device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd)
 // ---------------------------------------------------------------------------
 // plain lookup: out[i] = lookup(probes[i])
 // ---------------------------------------------------------------------------
+// A block processes tiles of kLookupItems * kBlock probes; item k of thread t
+// is probe tile + k * kBlock + t (coalesced), and the kLookupItems probes of a
+// thread are searched in lockstep.
+#ifndef GJ_LOOKUP_ITEMS
+#define GJ_LOOKUP_ITEMS 8
+#endif
+constexpr int kLookupItems = GJ_LOOKUP_ITEMS;
+
 template <class Op>
-__global__ void __launch_bounds__(kBlock) k_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_lookup(const Op op, const stage_desc sd,
                                                    const uint64_t* __restrict__ probes, uint64_t m,
                                                    uint32_t* __restrict__ out) {
     extern __shared__ uint64_t cache[];
     stage_cache(cache, sd);
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // two independent probes per iteration keep more loads in flight
-    for (; i + stride < m; i += 2 * stride) {
-        const uint64_t k0 = __ldcs(reinterpret_cast<const unsigned long long*>(probes + i));
-        const uint64_t k1 = __ldcs(reinterpret_cast<const unsigned long long*>(probes + i + stride));
-        const uint32_t r0 = op(cache, k0);
-        const uint32_t r1 = op(cache, k1);
-        __stcs(out + i, r0);
-        __stcs(out + i + stride, r1);
-    }
-    if (i < m) {
-        const uint64_t k0 = __ldcs(reinterpret_cast<const unsigned long long*>(probes + i));
-        __stcs(out + i, op(cache, k0));
+    constexpr uint64_t tile = (uint64_t)kLookupItems * kBlock;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < m; t0 += (uint64_t)gridDim.x * tile) {
+        uint64_t key[kLookupItems];
+        uint32_t res[kLookupItems];
+#pragma unroll
+        for (int k = 0; k < kLookupItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
+        }
+        op.template batch<kLookupItems>(cache, key, res);
+#pragma unroll
+        for (int k = 0; k < kLookupItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            if (i < m) __stcs(out + i, res[k]);
+        }
     }
 }
 
 // scattered lookup over a partitioned relation: out[rows[i]] = lookup(keys[i])
 template <class Op>
-__global__ void __launch_bounds__(kBlock) k_scatter_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_scatter_lookup(const Op op, const stage_desc sd,
                                                            const uint64_t* __restrict__ keys,
                                                            const uint32_t* __restrict__ rows, uint64_t m,
                                                            uint32_t* __restrict__ out) {
     extern __shared__ uint64_t cache[];
     stage_cache(cache, sd);
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
-        const uint64_t k = __ldcs(reinterpret_cast<const unsigned long long*>(keys + i));
-        const uint32_t r = __ldcs(rows + i);
-        out[r] = op(cache, k);
+    constexpr uint64_t tile = (uint64_t)kLookupItems * kBlock;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < m; t0 += (uint64_t)gridDim.x * tile) {
+        uint64_t key[kLookupItems];
+        uint32_t res[kLookupItems];
+#pragma unroll
+        for (int k = 0; k < kLookupItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(keys + i)) : 0ull;
+        }
+        op.template batch<kLookupItems>(cache, key, res);
+#pragma unroll
+        for (int k = 0; k < kLookupItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            if (i < m) out[__ldcs(rows + i)] = res[k];
+        }
     }
 }
 
@@ -120,7 +168,8 @@ __global__ void __launch_bounds__(kBlock) k_scatter_lookup(const Op op, const st
 // counter, so every predecessor of a tile is already running when the tile
 // looks back: each wait ends.  Waits are bounded anyway; on expiry the kernel
 // raises the error flag (GJ_ERR_TIMEOUT on the host) and stops writing.
-constexpr int kItems = 8;
+constexpr int kItems = GJ_LOOKUP_ITEMS;
+static_assert(kItems >= 4 && (kItems & (kItems - 1)) == 0, "the pairs scan needs a power-of-two item count >= 4");
 constexpr uint32_t kTile = kBlock * kItems;
 constexpr unsigned long long kFlagAggregate = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
@@ -134,7 +183,7 @@ struct pairs_ws {
 };
 
 template <class Op>
-__global__ void __launch_bounds__(kBlock) k_pairs(const Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
+__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_pairs(const Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
                                                   const uint32_t* __restrict__ rows, uint64_t m,
                                                   uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
                                                   uint64_t* __restrict__ d_count, pairs_ws ws, uint32_t num_tiles) {
@@ -163,11 +212,17 @@ __global__ void __launch_bounds__(kBlock) k_pairs(const Op op, const stage_desc 
         uint32_t pos[kItems];
         uint32_t lane_rank[kItems];
         uint32_t flags = 0;
+        uint64_t key[kItems];
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            pos[k] = kInvalid;
-            if (i < m) pos[k] = op(cache, __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)));
+            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
+        }
+        op.template batch<kItems>(cache, key, pos);
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            if (i >= m) pos[k] = kInvalid;
             const bool hit = pos[k] != kInvalid;
             const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
             lane_rank[k] = __popc(ballot & ((1u << lane) - 1u));
@@ -301,7 +356,7 @@ template <class Op>
 int run_lookup(const Op& op, const stage_desc& sd, const uint64_t* probes, uint64_t m, uint32_t* out, cudaStream_t s) {
     const size_t smem = stage_bytes(sd);
     int grid = 0;
-    GJ_TRY(grid_for(k_lookup<Op>, smem, m, &grid));
+    GJ_TRY(grid_for(k_lookup<Op>, smem, (m + kLookupItems - 1) / kLookupItems, &grid));
     k_lookup<Op><<<grid, kBlock, smem, s>>>(op, sd, probes, m, out);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
@@ -312,7 +367,7 @@ int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const 
                 uint32_t* out, cudaStream_t s) {
     const size_t smem = stage_bytes(sd);
     int grid = 0;
-    GJ_TRY(grid_for(k_scatter_lookup<Op>, smem, m, &grid));
+    GJ_TRY(grid_for(k_scatter_lookup<Op>, smem, (m + kLookupItems - 1) / kLookupItems, &grid));
     k_scatter_lookup<Op><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, out);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;

@@ -174,6 +174,16 @@ int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk, const uint
                      const int64_t* d_price, const int64_t* d_discount, uint64_t nfact,
                      const uint8_t* d_dim_flag, uint32_t lo, uint32_t hi, int64_t* d_out, void* stream);
 
+/* ---- learned position model ---------------------------------------------- */
+/* The root MLP's backward pass as the learned index's trainer runs it:
+ * d_grad (same layout as d_params: W1[H] b1[H] W2[HxH, out-major] b2[H]
+ * W3[H] b3) receives the gradient of sum_s (mlp(x_s) - y_s)^2 over the
+ * count samples, *d_loss (device) that sum.  hidden in [1, 32].  Allocates
+ * its scratch internally; synchronous.  Exposed so that the gradient can be
+ * checked against an independent implementation. */
+int gj_learned_mlp_grad(const float* d_params, uint32_t hidden, const float* d_x, const float* d_y, uint64_t count,
+                        float* d_grad, double* d_loss, void* stream);
+
 /* ---- batched lookup stream ------------------------------------------------ */
 /* Many probe batches against several indexes (not in the reference).  Batch
  * b probes d_probes[probe_offset[b] .. +batch_size[b]) against

@@ -205,6 +205,8 @@ struct harmonia_view {
     uint64_t inner_size;     // 32 * inner node count
     uint32_t depth;
     uint32_t cached_nodes;   // leading nodes (level order) staged in shared memory
+    uint32_t cached_levels;  // the cached nodes are exactly the top cached_levels levels
+    uint32_t pad;
 };
 
 // shared cache layout: cached_nodes * 32 keys, then cached_nodes children
@@ -285,6 +287,249 @@ GJ_DEVICE_INLINE uint32_t rs_lookup(const rs_view& v, uint64_t key) {
     if ((pos == b && b > 0 && ld_ro(v.col + b - 1) >= key) || (pos == e && e < v.n && ld_ro(v.col + e) < key))
         pos = lower_bound_branch_free(v.col, v.n, key);
     return pos < v.n ? (uint32_t)pos : kInvalid;
+}
+
+// ---------------------------------------------------------------------------
+// batched lookups: K independent probes per thread searched in lockstep
+// ---------------------------------------------------------------------------
+// A probe's search is a chain of dependent loads, so one probe per thread
+// leaves the memory system idle while the thread waits.  The batched forms
+// advance K probes one search step at a time: the K loads of a step are
+// independent and are in flight together.  Results equal the single-probe
+// functions above.
+
+// branch-free lower bound of key[k] in arr[lo_k, lo_k + len_k) with
+// len_k <= 2^steps - 1 for all k
+template <int K>
+GJ_DEVICE_INLINE void lower_bound_bounded_batch(const uint64_t* arr, const uint64_t (&lo)[K], const uint32_t (&len)[K],
+                                                const uint64_t (&key)[K], int steps, uint32_t (&r)[K]) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) r[k] = 0;
+    for (int s = steps - 1; s >= 0; --s) {
+        const uint32_t w = 1u << s;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const uint32_t i = r[k] + w - 1;
+            r[k] += (i < len[k] && ld_ro(arr + lo[k] + i) < key[k]) ? w : 0u;
+        }
+    }
+}
+
+GJ_DEVICE_INLINE int steps_for(uint64_t len) {  // smallest s with len <= 2^s - 1
+    return len == 0 ? 0 : 64 - __clzll(len);
+}
+
+template <int K>
+GJ_DEVICE_INLINE void bs_lookup_batch(const bs_view& v, const uint64_t* fence, const uint64_t (&key)[K],
+                                      uint32_t (&res)[K]) {
+    uint64_t lo[K];
+    uint32_t len[K];
+    int steps;
+    if (v.fence_slots == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            lo[k] = 0;
+            len[k] = (uint32_t)v.n;
+        }
+        steps = steps_for(v.n);
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            uint32_t c = 0;
+            for (int s = (int)v.fence_steps - 1; s >= 0; --s) {
+                const uint32_t w = 1u << s;
+                c += (fence[c + w - 1] < key[k]) ? w : 0u;
+            }
+            c += (fence[c] < key[k]) ? 1u : 0u;
+            if (c == 0) {
+                lo[k] = 0;
+                len[k] = 0;
+            } else {
+                lo[k] = ((uint64_t)(c - 1) << v.fence_shift) + 1;
+                uint64_t hi = (uint64_t)c << v.fence_shift;
+                if (hi > v.n) hi = v.n;
+                len[k] = (uint32_t)(hi - lo[k]);
+            }
+        }
+        steps = (int)v.fence_shift;  // ranges hold at most 2^shift - 1 keys
+    }
+    uint32_t r[K];
+    lower_bound_bounded_batch<K>(v.col, lo, len, key, steps, r);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint64_t lb = lo[k] + r[k];
+        res[k] = lb < v.n ? (uint32_t)lb : kInvalid;
+    }
+}
+
+template <int LOGW, int K>
+GJ_DEVICE_INLINE void btree_lookup_batch(const btree_view& v, const uint64_t* cache, const uint64_t (&key)[K],
+                                         uint32_t (&res)[K]) {
+    constexpr uint32_t W = 1u << LOGW;
+    uint64_t tk[K];  // probes above the largest key walk the rightmost path
+    uint32_t j[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        tk[k] = key[k] > v.max_key ? v.max_key : key[k];
+        j[k] = 0;
+    }
+    const int h = (int)v.height;
+    const int first_global = h - (int)v.cached_levels;
+    for (int l = h; l >= 1; --l) {
+        uint32_t c[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) c[k] = 0;
+        if (l > first_global) {
+            const uint64_t* base = cache + v.smem_offset[l];
+#pragma unroll
+            for (int s = LOGW - 1; s >= 0; --s) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) c[k] += (base[j[k] * W + c[k] + (1u << s) - 1] < tk[k]) ? (1u << s) : 0u;
+            }
+        } else {
+            const uint64_t* base = v.level[l];
+#pragma unroll
+            for (int s = LOGW - 1; s >= 0; --s) {
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    c[k] += (ld_ro(base + (uint64_t)j[k] * W + c[k] + (1u << s) - 1) < tk[k]) ? (1u << s) : 0u;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) j[k] = j[k] * W + c[k];
+    }
+    uint64_t lo[K];
+    uint32_t len[K], r[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        lo[k] = (uint64_t)j[k] * W;
+        const uint64_t rem = v.n - lo[k];
+        len[k] = rem < W ? (uint32_t)rem : W;
+    }
+    lower_bound_bounded_batch<K>(v.col, lo, len, tk, LOGW, r);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint64_t pos = lo[k] + r[k];
+        res[k] = (key[k] <= v.max_key && r[k] < len[k] && ld_ro(v.col + pos) == key[k]) ? (uint32_t)pos : kInvalid;
+    }
+}
+
+template <int K>
+GJ_DEVICE_INLINE void harmonia_lookup_batch(const harmonia_view& v, const uint64_t* cache, const uint64_t (&key)[K],
+                                            uint32_t (&res)[K]) {
+    constexpr uint32_t NK = kHarmoniaKeys;
+    uint64_t pos[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) pos[k] = 0;
+    const uint32_t depth = v.depth;
+    for (uint32_t d = 1; d < depth; ++d) {
+        uint64_t child[K];
+        uint32_t lb[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) lb[k] = 0;
+        if (d <= v.cached_levels) {
+            const uint64_t* ch = cache + (uint64_t)v.cached_nodes * NK;
+#pragma unroll
+            for (int k = 0; k < K; ++k) child[k] = ch[pos[k]];
+#pragma unroll
+            for (int s = 4; s >= 0; --s) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) lb[k] += (cache[pos[k] * NK + lb[k] + (1u << s) - 1] < key[k]) ? (1u << s) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k) lb[k] += (cache[pos[k] * NK + lb[k]] < key[k]) ? 1u : 0u;
+        } else {
+            // the child offset only depends on the node: load it alongside the search
+#pragma unroll
+            for (int k = 0; k < K; ++k) child[k] = ld_ro(v.children + pos[k]);
+#pragma unroll
+            for (int s = 4; s >= 0; --s) {
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    lb[k] += (ld_ro(v.keys + pos[k] * NK + lb[k] + (1u << s) - 1) < key[k]) ? (1u << s) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                lb[k] += (lb[k] == NK - 1 && ld_ro(v.keys + pos[k] * NK + lb[k]) < key[k]) ? 1u : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) pos[k] = child[k] + lb[k];
+    }
+    uint64_t lo[K];
+    uint32_t len[K], r[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        lo[k] = (depth > 1) ? (pos[k] * NK - v.inner_size) : 0;
+        len[k] = NK;
+    }
+    // 32 keys: 5 steps cover 31, the sixth decides between 31 and 32
+    lower_bound_bounded_batch<K>(v.col, lo, len, key, 5, r);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        uint32_t rr = r[k];
+        if (rr == NK - 1 && ld_ro(v.col + lo[k] + rr) < key[k]) rr = NK;
+        const uint64_t p = lo[k] + rr;
+        res[k] = (p < v.n && ld_ro(v.col + p) == key[k]) ? (uint32_t)p : kInvalid;
+    }
+}
+
+template <int K>
+GJ_DEVICE_INLINE void rs_lookup_batch(const rs_view& v, const uint64_t (&key)[K], uint32_t (&res)[K]) {
+    // spline segment: radix table, then a short search over the segment's points
+    uint32_t lo[K], cnt[K];
+    bool inner[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        inner[k] = key[k] > v.min_key && key[k] < v.max_key;
+        const uint64_t prefix = inner[k] ? (key[k] - v.min_key) >> v.shift : 0;
+        lo[k] = ld_ro(v.table + prefix);
+        cnt[k] = inner[k] ? ld_ro(v.table + prefix + 1) - lo[k] : 0;
+    }
+    bool more = true;
+    while (more) {
+        more = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (cnt[k] > 0) {
+                const uint32_t step = cnt[k] >> 1, mid = lo[k] + step;
+                if (ld_ro(v.sx + mid) < key[k]) {
+                    lo[k] = mid + 1;
+                    cnt[k] -= step + 1;
+                } else {
+                    cnt[k] = step;
+                }
+                more |= cnt[k] > 0;
+            }
+        }
+    }
+    uint64_t b[K], e[K];
+    uint32_t len[K], r[K];
+    const double err = (double)v.max_error;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double est;
+        if (!inner[k]) {
+            est = key[k] <= v.min_key ? 0.0 : (double)(v.n - 1);
+        } else {
+            const uint64_t dx0 = ld_ro(v.sx + lo[k] - 1), ux = ld_ro(v.sx + lo[k]);
+            const double dy0 = ld_ro(v.sy + lo[k] - 1), uy = ld_ro(v.sy + lo[k]);
+            const double slope = (uy - dy0) / (double)(ux - dx0);
+            est = __dadd_rn(__dmul_rn((double)(key[k] - dx0), slope), dy0);
+        }
+        b[k] = est < err ? 0 : (uint64_t)(est - err);
+        e[k] = (est + err + 2 > (double)v.n) ? v.n : (uint64_t)(est + err + 2);
+        if (b[k] > e[k]) b[k] = e[k];
+        len[k] = (uint32_t)(e[k] - b[k]);
+    }
+    lower_bound_bounded_batch<K>(v.col, b, len, key, steps_for(2ull * v.max_error + 3), r);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        uint64_t pos = b[k] + r[k];
+        if ((pos == b[k] && b[k] > 0 && ld_ro(v.col + b[k] - 1) >= key[k]) ||
+            (pos == e[k] && e[k] < v.n && ld_ro(v.col + e[k]) < key[k]))
+            pos = lower_bound_branch_free(v.col, v.n, key[k]);
+        res[k] = pos < v.n ? (uint32_t)pos : kInvalid;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -386,6 +631,45 @@ GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* roo
     if ((pos == b && b > 0 && ld_ro(v.col + b - 1) >= key) || (pos == e && e < v.n && ld_ro(v.col + e) < key))
         pos = lower_bound_branch_free(v.col, v.n, key);  // exact fallback: the plain binary search
     return pos < v.n ? (uint32_t)pos : kInvalid;
+}
+
+template <int K>
+GJ_DEVICE_INLINE void learned_lookup_batch(const learned_view& v, const float* root, const uint64_t (&key)[K],
+                                           uint32_t (&res)[K]) {
+    uint64_t b[K], e[K];
+    uint32_t len[K], r[K], maxlen = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint32_t li = learned_route(v, root, learned_norm(v, key[k]));
+        const uint64_t* lp = reinterpret_cast<const uint64_t*>(v.leaves + li);
+        learned_leaf lf;
+        lf.x0 = ld_ro(lp);
+        const uint64_t w1 = ld_ro(lp + 1), w2 = ld_ro(lp + 2);
+        lf.base = (uint32_t)w1;
+        lf.slope = __uint_as_float((uint32_t)(w1 >> 32));
+        lf.err_lo = (uint32_t)w2;
+        lf.err_hi = (uint32_t)(w2 >> 32);
+        const int64_t pred = learned_predict(lf, key[k]);
+        int64_t lo = pred - (int64_t)lf.err_lo;
+        int64_t hi = pred + (int64_t)lf.err_hi + 1;
+        const int64_t n = (int64_t)v.n;
+        if (lo < 0) lo = 0;
+        if (hi > n) hi = n;
+        if (lo > hi) lo = hi;
+        b[k] = (uint64_t)lo;
+        e[k] = (uint64_t)hi;
+        len[k] = (uint32_t)(e[k] - b[k]);
+        maxlen = len[k] > maxlen ? len[k] : maxlen;
+    }
+    lower_bound_bounded_batch<K>(v.col, b, len, key, steps_for(maxlen), r);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        uint64_t pos = b[k] + r[k];
+        if ((pos == b[k] && b[k] > 0 && ld_ro(v.col + b[k] - 1) >= key[k]) ||
+            (pos == e[k] && e[k] < v.n && ld_ro(v.col + e[k]) < key[k]))
+            pos = lower_bound_branch_free(v.col, v.n, key[k]);  // exact fallback: the plain binary search
+        res[k] = pos < v.n ? (uint32_t)pos : kInvalid;
+    }
 }
 
 }  // namespace gj

@@ -1,0 +1,95 @@
+"""Learned position model: GPU gradients against the CPU oracle, exact
+lookups, and what the trained root buys over the untrained (linear) one."""
+import numpy as np
+import pytest
+
+from test_lookup_gpu import column, from_dev_u32, probes_for, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def nparams(H):
+    return 2 * H + H * H + H + H + 1
+
+
+@pytest.mark.parametrize("H", [1, 8, 32])
+def test_mlp_gradient_matches_oracle(orc, gj, cuda, H):
+    import torch
+
+    rng = np.random.default_rng(H)
+    P = rng.normal(0, 0.5, nparams(H)).astype(np.float32)
+    x = rng.random(3000).astype(np.float32)
+    y = np.sort(rng.random(3000)).astype(np.float32)
+    g, loss = gj.learned_mlp_grad(torch.from_numpy(P).cuda(), H, torch.from_numpy(x).cuda(),
+                                  torch.from_numpy(y).cuda())
+    eloss, eg = orc.mlp_loss_grad(P, H, x, y)
+    g = g.cpu().numpy().astype(np.float64)
+    # float32 accumulation over 3000 samples against the oracle's float64
+    scale = np.abs(eg).max()
+    np.testing.assert_allclose(g, eg, rtol=2e-3, atol=2e-4 * scale)
+    assert abs(loss.item() - eloss) <= 1e-3 * max(1.0, eloss)
+
+
+@pytest.mark.parametrize("dist", [0, 1, 2])
+@pytest.mark.parametrize("root", [0, 1])
+def test_learned_lookup_exact(orc, gj, cuda, dist, root):
+    import torch
+
+    n = 1 << 18
+    keys = gj.generate_sorted_keys(n, dist, 1 << 63, seed=dist + 40)
+    probes = gj.generate_probes(keys, 1 << 17, theta=0.0, absent_fraction=0.05, seed=41)
+    ix = gj.learned_index(learned_root=root, learned_leaves=4096, learned_steps=200).construct(None, keys)
+    got = from_dev_u32(ix.lookup(probes))
+    col = keys.cpu().numpy().view(np.uint64)
+    pr = probes.cpu().numpy().view(np.uint64)
+    np.testing.assert_array_equal(got, orc.bs_lookup(col, pr))
+    # also the edge probes
+    rng = np.random.default_rng(3)
+    edge = probes_for(rng, col, 1000)
+    np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, edge))), orc.bs_lookup(col, edge))
+    max_err, mean_window = ix.stats()
+    assert mean_window >= 1.0 and max_err >= 0
+
+
+def test_learned_small_and_ragged(orc, gj, cuda):
+    import torch
+
+    rng = np.random.default_rng(12)
+    for n in (1, 2, 3, 100, 4097):
+        col = column(rng, n)
+        pr = probes_for(rng, col, 500)
+        for root in (0, 1):
+            ix = gj.learned_index(learned_root=root, learned_leaves=64, learned_steps=20).construct(None,
+                                                                                                  to_dev(torch, col))
+            np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), orc.bs_lookup(col, pr),
+                                          err_msg=f"n={n} root={root}")
+
+
+def test_trained_root_beats_linear_root_on_lognormal(gj, cuda):
+    n = 1 << 20
+    keys = gj.generate_sorted_keys(n, 1, 1 << 63, seed=77)
+    lin = gj.learned_index(learned_root=0, learned_leaves=4096).construct(None, keys)
+    mlp = gj.learned_index(learned_root=1, learned_leaves=4096, learned_steps=600).construct(None, keys)
+    _, w_lin = lin.stats()
+    _, w_mlp = mlp.stats()
+    # the trained network routes keys by their learned CDF; the linear root
+    # crowds the dense low end of the lognormal keys into few leaves
+    assert w_mlp < 0.5 * w_lin, (w_mlp, w_lin)
+
+
+def test_learned_in_pairs_and_partitioned(orc, gj, cuda):
+    n = 1 << 16
+    keys = gj.generate_sorted_keys(n, 0, 1 << 63, seed=5)
+    probes = gj.generate_probes(keys, 50000, theta=0.5, absent_fraction=0.05, seed=6)
+    ix = gj.learned_index(learned_leaves=1024, learned_steps=100).construct(None, keys)
+    col = keys.cpu().numpy().view(np.uint64)
+    pr = probes.cpu().numpy().view(np.uint64)
+    exp = orc.bs_lookup(col, pr)
+    pos, _, _ = ix.partitioned_inlj(probes)
+    np.testing.assert_array_equal(from_dev_u32(pos), exp)
+    out, cnt = ix.inlj_pairs(probes)
+    c = int(cnt.item())
+    got = out[: 2 * c].cpu().numpy().view(np.uint32).reshape(-1, 2)
+    erows, epos = orc.pairs_from_positions(exp)
+    np.testing.assert_array_equal(got[:, 0], erows)
+    np.testing.assert_array_equal(got[:, 1], epos)
