@@ -205,11 +205,8 @@ def cpu_baseline_btree(h_keys, h_probes, sample: int):
                       f"(oracle B+tree, reference page geometry 247/246), {threads} threads, {dt:.2f} s"}
 
 
-def gpu_main(args):
-    import numpy as np
+def gpu_setup():
     import torch
-
-    import gpujoin_gb300 as gj
 
     world, rank, local = dist_env()
     if world > 1:
@@ -217,7 +214,23 @@ def gpu_main(args):
         init_dist("nccl")
     device = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(device)
-    stream = torch.cuda.current_stream(device)
+    return world, rank, device, torch.cuda.current_stream(device)
+
+
+def gpu_main(args):
+    world, rank, device, stream = gpu_setup()
+    fn = {"inlj": inlj_workload, "partitioned": partitioned_workload, "star": star_workload,
+          "learned": learned_workload, "batch": batch_workload}[args.workload]
+    line = fn(args, world, rank, device, stream)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def inlj_workload(args, world, rank, device, stream):
+    import numpy as np
+    import torch
+
+    import gpujoin_gb300 as gj
 
     n, m = 1 << args.n_log2, 1 << args.m_log2
     keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
@@ -319,8 +332,280 @@ def gpu_main(args):
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
+
+
+# ---------------------------------------------------------------------------
+# further workloads (run with --workload; the default line is inlj)
+# ---------------------------------------------------------------------------
+def _base_line(args, world, metric, value, unit, ms_per_step, workload, extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded device generators)",
+            "config": {"workload": workload, "parallelism": f"replicas x{world}"}}
+    line.update(extra)
+    return line
+
+
+def partitioned_workload(args, world, rank, device, stream):
+    """Partitioned INLJ at out-of-L2 scale: 2^28-key index, 2^29 Zipf(0.5)
+    probes, range partition with an autotuned fanout (2^8..2^12) and window,
+    pairs emitted in partition order."""
+    import ctypes
+
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    n_log2 = args.n_log2 if args.n_log2 != 26 else 28
+    m_log2 = args.m_log2 if args.m_log2 != 28 else 29
+    n, m = 1 << n_log2, 1 << m_log2
+    keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
+    probes = gj.generate_probes(keys, m, theta=args.theta, seed=args.seed + 1)
+    ix = gj.make_index(args.indexes.split(",")[0]).construct(None, keys)
+    pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device)
+
+    # autotune fanout and window on a sample of the probes
+    sample = probes[: 1 << min(m_log2, 25)]
+    best = None
+    tune = {}
+    for bits in (8, 10, 12):
+        for window in (sample.numel(), sample.numel() // 4):
+            need = ctypes.c_size_t()
+            gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
+            ws = torch.empty(need.value, dtype=torch.uint8, device=device)
+
+            def run():
+                gj._check(gj.lib().gj_partitioned_inlj(ix.handle, sample.data_ptr(), sample.numel(), window, bits,
+                                                        None, pairs.data_ptr(), count.data_ptr(), ws.data_ptr(),
+                                                        ws.numel(), stream.cuda_stream))
+
+            t = time_steps(run, 2, 1, stream, 1, device) / 2
+            tune[f"bits{bits}_window{window}"] = round(t, 3)
+            if best is None or t < best[0]:
+                best = (t, bits, window / sample.numel())
+            del ws
+    _, bits, wfrac = best
+    window = max(1, int(m * wfrac))
+    need = ctypes.c_size_t()
+    gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
+    ws = torch.empty(need.value, dtype=torch.uint8, device=device)
+
+    def step():
+        gj._check(gj.lib().gj_partitioned_inlj(ix.handle, probes.data_ptr(), m, window, bits, None,
+                                                pairs.data_ptr(), count.data_ptr(), ws.data_ptr(), ws.numel(),
+                                                stream.cuda_stream))
+
+    sampler = ClockSampler(device.index)
+    sampler.start()
+    ms = time_steps(step, args.steps, args.warmup, stream, world, device)
+    clocks = sampler.stop()
+    ms = max_over_ranks(ms, world, device)
+    got = int(count.item())
+
+    # the same probes through the unpartitioned pairs kernel, for comparison
+    pw = ctypes.c_size_t()
+    gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(pw))
+    pws = torch.empty(pw.value, dtype=torch.uint8, device=device)
+    plain_ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, pws), max(2, args.steps // 2), 1, stream, world,
+                          device) / max(2, args.steps // 2)
+
+    per_step = ms / args.steps
+    bpp = 8 + 12 + 12 + 8 + 8.0 * n / m
+    peak, peak_kind = measured_peak()
+    achieved = bpp * m / (per_step / 1e3) / 1e9
+    windows = (m + window - 1) // window
+    return _base_line(
+        args, world, "partitioned INLJ probe tuples/s (1 GB300 per rank), % of HBM roofline",
+        world * m * args.steps / (ms / 1e3), "probe tuples/s", per_step,
+        f"partitioned INLJ: {n} uniform uint64 keys (2^{n_log2}), {m} Zipf({args.theta}) probes (2^{m_log2}), "
+        f"{ix.type_name()}, range partition 2^{bits}, window {window}",
+        {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune_ms": tune,
+                         "plain_pairs_ms_per_step": plain_ms,
+                         "plain_pairs_tuples_per_s": m / (plain_ms / 1e3)},
+         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                      "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_probe": bpp,
+                      "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
+         "gpu_launches": args.steps * windows * 6, "clocks": clocks, "cpu_baseline": None, "e2e": None})
+
+
+def star_inputs(n_fact, n_dim, seed, device):
+    import torch
+
+    g = torch.Generator(device="cpu")
+    g.manual_seed(seed)
+    dim_keys = torch.arange(1, n_dim + 1, dtype=torch.int64)
+    flag = torch.zeros(n_dim, dtype=torch.uint8)
+    flag[torch.randperm(n_dim, generator=g)[: n_dim // 6]] = 1
+    fk = torch.randint(1, n_dim + 1, (n_fact,), generator=g, dtype=torch.int32)
+    date = torch.randint(0, 2556, (n_fact,), generator=g, dtype=torch.int32)
+    price = torch.randint(90000, 10500001, (n_fact,), generator=g, dtype=torch.int64)
+    disc = torch.randint(0, 11, (n_fact,), generator=g, dtype=torch.int64)
+    return [t.to(device) for t in (dim_keys, flag, fk, date, price, disc)]
+
+
+def star_workload(args, world, rank, device, stream):
+    """Star-join aggregate: 6M fact rows, 200k-row dimension indexed by a
+    B+tree, 30-day date window, exact int64 sums."""
+    import numpy as np
+    import torch
+
+    import gpujoin_gb300 as gj
+    import oracle
+
+    n_fact, n_dim, lo, hi = 6_000_000, 200_000, 1000, 1030
+    dim_keys, flag, fk, date, price, disc = star_inputs(n_fact, n_dim, args.seed, device)
+    ix = gj.btree_index().construct(None, dim_keys)
+    out = torch.zeros(2, dtype=torch.int64, device=device)
+    ms = time_steps(lambda: gj.star_join_sum(ix, fk, date, price, disc, flag, lo, hi, out), args.steps, args.warmup,
+                    stream, world, device)
+    ms = max_over_ranks(ms, world, device)
+    got = out.cpu().numpy()
+    num, den = oracle.star_join(fk.cpu().numpy().view(np.uint32), date.cpu().numpy().view(np.uint32),
+                                price.cpu().numpy(), disc.cpu().numpy(), dim_keys.cpu().numpy().view(np.uint64),
+                                flag.cpu().numpy(), lo, hi)
+    per_step = ms / args.steps
+    bytes_per_row = 4 + (30 / 2556) * (4 + 8 + 8 + 32)
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_row * n_fact / (per_step / 1e3) / 1e9
+    return _base_line(
+        args, world, "star-join fact rows/s (1 GB300 per rank)", world * n_fact * args.steps / (ms / 1e3),
+        "fact rows/s", per_step,
+        f"star join: {n_fact} fact rows, {n_dim} dimension rows (B+tree), 30-day window of 2556 days",
+        {"star": {"sums": [int(got[0]), int(got[1])], "oracle_sums": [num, den],
+                  "exact": bool(int(got[0]) == num and int(got[1]) == den), "latency_us": per_step * 1e3},
+         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                      "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_row": bytes_per_row,
+                      "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
+         "gpu_launches": args.steps, "cpu_baseline": None, "e2e": None})
+
+
+def learned_workload(args, world, rank, device, stream):
+    """Learned index against binary search and RadixSpline at exact outputs:
+    2^27 keys from three distributions, 2^28 uniformly sampled probes with 5%
+    absent keys, lower-bound positions."""
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    n_log2 = args.n_log2 if args.n_log2 != 26 else 27
+    n, m = 1 << n_log2, 1 << args.m_log2
+    results = {}
+    out = torch.empty(m, dtype=torch.int32, device=device)
+    ref = torch.empty(m, dtype=torch.int32, device=device)
+    for dist_name, dist in (("uniform", gj.DIST_UNIFORM), ("lognormal", gj.DIST_LOGNORMAL),
+                            ("clusters", gj.DIST_CLUSTERS)):
+        keys = gj.generate_sorted_keys(n, dist, 1 << 63, seed=args.seed + dist)
+        probes = gj.generate_probes(keys, m, theta=0.0, absent_fraction=0.05, seed=args.seed + 10 + dist)
+        row = {}
+        bs = gj.binary_search_index().construct(None, keys)
+        bs.lookup(probes, ref)
+        for kind, kw in (("binary_search", {}), ("radix_spline", {}), ("learned_mlp", {"learned_root": 1}),
+                         ("learned_linear", {"learned_root": 0})):
+            t0 = time.perf_counter()
+            ix = gj.make_index(kind.split("_")[0] if kind.startswith("learned") else kind, **kw).construct(None, keys)
+            torch.cuda.synchronize()
+            build_s = time.perf_counter() - t0
+            ms = time_steps(lambda: ix.lookup(probes, out), args.steps, args.warmup, stream, world, device)
+            exact = bool(torch.equal(out, ref))
+            entry = {"tuples_per_s": m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "exact": exact,
+                     "build_s": round(build_s, 3), "index_bytes": ix.memory_consumption()}
+            if kind.startswith("learned"):
+                me, mw = ix.stats()
+                entry.update({"max_error": me, "mean_window": round(mw, 2)})
+            row[kind] = entry
+            ix.free()
+        results[dist_name] = row
+        del keys, probes
+    head = results["uniform"]["learned_mlp"]
+    return _base_line(
+        args, world, "learned-index probe tuples/s (1 GB300 per rank), exact lower bounds",
+        world * head["tuples_per_s"], "probe tuples/s", head["ms_per_step"],
+        f"learned vs plain: {n} keys (2^{n_log2}) x 3 distributions, {m} probes (2^{args.m_log2}) with 5% absent",
+        {"learned": results, "roofline": None, "gpu_launches": args.steps, "cpu_baseline": None, "e2e": None})
+
+
+def batch_workload(args, world, rank, device, stream):
+    """Batched lookup stream: 8 indexes (B+tree, Harmonia, RadixSpline,
+    learned; 2^20..2^27 keys), 4096 batches of lognormal size in [1k, 16M]
+    drawn Zipf(0.8) against their index, admitted in rounds by an HBM budget;
+    one persistent kernel against one launch per batch."""
+    import numpy as np
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    rng = np.random.default_rng(args.seed)
+    specs = [("btree", 27, 0), ("harmonia", 26, 0), ("radix_spline", 25, 1), ("learned", 24, 1),
+             ("btree", 23, 1), ("harmonia", 22, 0), ("radix_spline", 21, 0), ("learned", 20, 0)]
+    indexes, cols = [], []
+    for i, (kind, lg, dist) in enumerate(specs):
+        keys = gj.generate_sorted_keys(1 << lg, dist, 1 << 63, seed=args.seed + 100 + i)
+        indexes.append(gj.make_index(kind).construct(None, keys))
+        cols.append(keys)
+    nb = 4096
+    sizes = np.clip(np.exp(rng.normal(np.log(65536), 1.6, nb)), 1000, 16 << 20).astype(np.int64)
+    which = rng.integers(0, len(specs), nb).astype(np.uint32)
+    budget = 2 << 30  # probe bytes admitted per round
+    rounds, cur, cur_bytes = [], [], 0
+    for b in range(nb):
+        if cur and cur_bytes + 8 * sizes[b] > budget:
+            rounds.append(cur)
+            cur, cur_bytes = [], 0
+        cur.append(b)
+        cur_bytes += 8 * int(sizes[b])
+    rounds.append(cur)
+    max_round = max(int(sizes[r].sum()) for r in rounds)
+    probes = torch.empty(max_round, dtype=torch.int64, device=device)
+    out = torch.empty(max_round, dtype=torch.int32, device=device)
+    done = torch.zeros(nb, dtype=torch.int64, device=device)
+    import ctypes
+    need = ctypes.c_size_t()
+    gj.lib().gj_batch_workspace_size(len(indexes), nb, ctypes.byref(need))
+    ws = torch.empty(need.value, dtype=torch.uint8, device=device)
+    total = int(sizes.sum())
+    res = {}
+    for mode in (0, 1):
+        lat = []
+        t_all = 0.0
+        for r in rounds:
+            bs = sizes[r]
+            offs = np.concatenate([[0], np.cumsum(bs)[:-1]]).astype(np.uint64)
+            for j, b in enumerate(r):
+                probes[offs[j]: offs[j] + bs[j]] = gj.generate_probes(cols[which[b]], int(bs[j]), theta=0.8,
+                                                                       seed=args.seed + int(b))
+            start_ev = torch.cuda.Event(enable_timing=True)
+            end_ev = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+
+            def run():
+                gj.batch_lookup(indexes, which[r], offs, bs, probes, out, mode=mode, d_done_ns=done[: len(r)],
+                                workspace=ws)
+
+            run()  # warm
+            torch.cuda.synchronize()
+            start_ns = None
+            start_ev.record(stream)
+            stamp = torch.zeros(1, dtype=torch.int64, device=device)
+            run()
+            end_ev.record(stream)
+            torch.cuda.synchronize()
+            t_all += start_ev.elapsed_time(end_ev)
+            d = done[: len(r)].cpu().numpy().astype(np.int64)
+            lat.extend(((d - d.min()) / 1e3 + 0.0).tolist())
+        lat = np.array(lat)
+        res["persistent" if mode == 0 else "per_launch"] = {
+            "tuples_per_s": total / (t_all / 1e3), "ms_total": t_all,
+            "p50_batch_completion_us": float(np.percentile(lat, 50)),
+            "p99_batch_completion_us": float(np.percentile(lat, 99))}
+    head = res["persistent"]
+    return _base_line(
+        args, world, "batched lookup stream probe tuples/s (1 GB300 per rank)", world * head["tuples_per_s"],
+        "probe tuples/s", head["ms_total"],
+        f"batched stream: 8 indexes (2^20..2^27 keys), {nb} batches, {total} probes, {len(rounds)} admission rounds",
+        {"batch": res, "roofline": None, "gpu_launches": len(rounds), "cpu_baseline": None, "e2e": None})
 
 
 # ---------------------------------------------------------------------------
@@ -380,7 +665,7 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["inlj"], default="inlj")
+    ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch"], default="inlj")
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)
     ap.add_argument("--theta", type=float, default=0.5)

@@ -606,7 +606,10 @@ GJ_DEVICE_INLINE uint32_t learned_route(const learned_view& v, const float* root
 // leaf prediction (signed, may lie outside [0, n))
 GJ_DEVICE_INLINE int64_t learned_predict(const learned_leaf& lf, uint64_t key) {
     const float dx = (key >= lf.x0) ? (float)(key - lf.x0) : -(float)(lf.x0 - key);
-    return (int64_t)lf.base + (int64_t)floorf(lf.slope * dx);
+    // |offset| is kept below 2^62 so that pred +- err cannot overflow
+    float off = floorf(lf.slope * dx);
+    off = fminf(fmaxf(off, -4.0e18f), 4.0e18f);
+    return (int64_t)lf.base + (int64_t)off;
 }
 
 GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* root, uint64_t key) {
@@ -620,11 +623,13 @@ GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* roo
     lf.err_lo = (uint32_t)w2;
     lf.err_hi = (uint32_t)(w2 >> 32);
     const int64_t pred = learned_predict(lf, key);
+    const int64_t n = (int64_t)v.n;
+    // window [pred - err_lo, pred + err_hi + 1) clamped to [0, n]; a probe far
+    // outside the leaf's keys can push both ends below 0 or above n
     int64_t lo = pred - (int64_t)lf.err_lo;
     int64_t hi = pred + (int64_t)lf.err_hi + 1;
-    const int64_t n = (int64_t)v.n;
-    if (lo < 0) lo = 0;
-    if (hi > n) hi = n;
+    lo = lo < 0 ? 0 : (lo > n ? n : lo);
+    hi = hi < 0 ? 0 : (hi > n ? n : hi);
     if (lo > hi) lo = hi;
     const uint64_t b = (uint64_t)lo, e = (uint64_t)hi;
     uint64_t pos = b + lower_bound_branch_free(v.col + b, e - b, key);
@@ -650,11 +655,11 @@ GJ_DEVICE_INLINE void learned_lookup_batch(const learned_view& v, const float* r
         lf.err_lo = (uint32_t)w2;
         lf.err_hi = (uint32_t)(w2 >> 32);
         const int64_t pred = learned_predict(lf, key[k]);
+        const int64_t n = (int64_t)v.n;
         int64_t lo = pred - (int64_t)lf.err_lo;
         int64_t hi = pred + (int64_t)lf.err_hi + 1;
-        const int64_t n = (int64_t)v.n;
-        if (lo < 0) lo = 0;
-        if (hi > n) hi = n;
+        lo = lo < 0 ? 0 : (lo > n ? n : lo);  // clamp both ends to [0, n]
+        hi = hi < 0 ? 0 : (hi > n ? n : hi);
         if (lo > hi) lo = hi;
         b[k] = (uint64_t)lo;
         e[k] = (uint64_t)hi;

@@ -29,12 +29,12 @@ def test_batch_modes_match_oracle(orc, gj, cuda):
     probes = torch.empty(total, dtype=torch.int64, device="cuda")
     for b in range(nb):
         if sizes[b]:
-            probes[offs[b]: offs[b] + sizes[b]] = gj.generate_probes(cols[which[b]], int(sizes[b]), theta=0.8,
+            probes[int(offs[b]): int(offs[b]) + int(sizes[b])] = gj.generate_probes(cols[which[b]], int(sizes[b]), theta=0.8,
                                                                      absent_fraction=0.05, seed=b)
     h_probes = probes.cpu().numpy().view(np.uint64)
     exp = np.empty(total, dtype=np.uint32)
     for b in range(nb):
-        a, e = int(offs[b]), int(offs[b] + sizes[b])
+        a, e = int(offs[b]), int(offs[b]) + int(sizes[b])
         col = cols[which[b]].cpu().numpy().view(np.uint64)
         kind = specs[which[b]][0]
         exp[a:e] = (orc.exact_lookup if kind in ("btree", "harmonia") else orc.bs_lookup)(col, h_probes[a:e])
