@@ -103,6 +103,7 @@ _SIGNATURES = {
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
@@ -276,6 +277,14 @@ class abstract_index:
             workspace = _workspace(need.value, dev)
         _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
                                    _ptr(workspace), workspace.numel(), _stream(stream)))
+        return out_pairs, out_count
+
+    def inlj_pairs_noalloc(self, d_probes, out_pairs, out_count, stream=None):
+        """inlj_pairs without a workspace: the scratch is a fixed array inside the
+        library, for callers that cannot allocate while probing (at most
+        2^28 probes per call; overlapping calls must be serialised)."""
+        _check(lib().gj_inlj_pairs_noalloc(self.handle, _ptr(d_probes), d_probes.numel(), _ptr(out_pairs),
+                                           _ptr(out_count), _stream(stream)))
         return out_pairs, out_count
 
     def partitioned_inlj(self, d_probes, window_size: int = 0, radix_bits: int = 0, positions: bool = True,

@@ -133,6 +133,21 @@ int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Same pairs as gj_inlj_pairs, for callers that cannot allocate device
+ * memory when they probe (a frozen allocator, someone else's memory arena,
+ * or a probe path that must not call cudaMalloc/cudaFree because they
+ * synchronise the device).  No counterpart in the reference.  Its scratch is a
+ * fixed array inside the library (about 2 MiB on every GPU that loads the
+ * library, held until the process exits), so it needs no workspace argument
+ * and allocates nothing.  At most GJ_NOALLOC_MAX_PROBES probes per call;
+ * larger m returns GJ_ERR_TOO_LARGE.  The first call on a device looks up the
+ * array's device address: make it before capturing a stream.  All calls
+ * share the array: calls whose kernels overlap on the GPU (other streams,
+ * other host threads) must be serialised by the caller. */
+#define GJ_NOALLOC_MAX_PROBES (1ull << 28)
+int gj_inlj_pairs_noalloc(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                          uint64_t* d_count, void* stream);
+
 /* ---- partitioned INLJ ---------------------------------------------------- */
 /* Range partition of the probe side, replacing gpu_contiguous_prefix_sum_int64
  * + gpu_chunked_laswwc_radix_partition_int64_int64 as called from
