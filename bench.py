@@ -205,6 +205,17 @@ def cpu_baseline_btree(h_keys, h_probes, sample: int):
                       f"(oracle B+tree, reference page geometry 247/246), {threads} threads, {dt:.2f} s"}
 
 
+def index_params(args, kind):
+    """Build parameters given on the command line for an index kind."""
+    p = {}
+    if kind == "btree":
+        if args.btree_node_keys:
+            p["btree_node_keys"] = args.btree_node_keys
+        if args.btree_leaf_keys:
+            p["btree_leaf_keys"] = args.btree_leaf_keys
+    return p
+
+
 def gpu_setup():
     import torch
 
@@ -250,7 +261,7 @@ def inlj_workload(args, world, rank, device, stream):
     clocks = None
     for kind in kinds:
         t_build = time.perf_counter()
-        ix = gj.make_index(kind).construct(None, keys)
+        ix = gj.make_index(kind, **index_params(args, kind)).construct(None, keys)
         torch.cuda.synchronize()
         t_build = time.perf_counter() - t_build
 
@@ -672,6 +683,8 @@ def parse_args(argv=None):
     ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
+    ap.add_argument("--btree-node-keys", type=int, default=0, help="B+tree inner node width (0 = library default)")
+    ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     return ap.parse_args(argv)

@@ -67,6 +67,7 @@ class gj_index_params(ctypes.Structure):
     _fields_ = [
         ("struct_size", ctypes.c_uint32),
         ("btree_node_keys", ctypes.c_uint32),
+        ("btree_leaf_keys", ctypes.c_uint32),
         ("rs_radix_bits", ctypes.c_uint32),
         ("rs_max_error", ctypes.c_uint32),
         ("bs_cache_keys", ctypes.c_uint32),
@@ -100,6 +101,7 @@ _SIGNATURES = {
     "gj_index_get_type": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "gj_index_size": (_u64, [_vp]),
     "gj_index_learned_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)]),
+    "gj_index_device_view": (_i32, [_vp, _vp, _sz]),
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
@@ -324,7 +326,7 @@ class abstract_index:
 
 
 class btree_index(abstract_index):
-    """btree_index (src/indexes.cuh:93-147): clustered B+tree, 64-key nodes by default."""
+    """btree_index (src/indexes.cuh:93-147): clustered B+tree (node and leaf widths are build parameters)."""
 
     index_type = index_type_enum.btree
 

@@ -27,7 +27,7 @@ constexpr uint64_t kBatchTile = (uint64_t)kBatchBlock * kBatchItems;
 
 struct any_view {
     int32_t type;
-    uint32_t logw;
+    uint32_t pad;
     union {
         bs_view bs;
         btree_view bt;
@@ -59,9 +59,13 @@ __device__ __forceinline__ uint32_t any_lookup(const any_view& v, uint64_t key) 
             return bs_lookup(b, nullptr, key);
         }
         case GJ_INDEX_BTREE:
-            if (v.logw == 4) return btree_lookup<4>(v.u.bt, nullptr, key);
-            if (v.logw == 5) return btree_lookup<5>(v.u.bt, nullptr, key);
-            return btree_lookup<6>(v.u.bt, nullptr, key);
+            switch (v.u.bt.node_keys) {
+                case 4: return btree_lookup<4>(v.u.bt, nullptr, key);
+                case 8: return btree_lookup<8>(v.u.bt, nullptr, key);
+                case 16: return btree_lookup<16>(v.u.bt, nullptr, key);
+                case 32: return btree_lookup<32>(v.u.bt, nullptr, key);
+                default: return btree_lookup<64>(v.u.bt, nullptr, key);
+            }
         case GJ_INDEX_HARMONIA: return harmonia_lookup(v.u.hm, nullptr, key);
         case GJ_INDEX_RADIX_SPLINE: return rs_lookup(v.u.rs, key);
         case GJ_INDEX_LEARNED: return learned_lookup(v.u.ln, v.u.ln.root, key);
@@ -178,7 +182,6 @@ int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32
         any_view& v = views[i];
         std::memset(&v, 0, sizeof(v));
         v.type = ix->type;
-        v.logw = ix->bt_logw;
         switch (ix->type) {
             case GJ_INDEX_BINARY_SEARCH: v.u.bs = ix->bs; break;
             case GJ_INDEX_BTREE: v.u.bt = ix->bt; v.u.bt.cached_levels = 0; break;

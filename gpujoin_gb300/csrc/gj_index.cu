@@ -80,12 +80,14 @@ __global__ void k_gather_fence(const uint64_t* __restrict__ col, uint64_t n, uin
     }
 }
 
-// B+tree level l: slot k = max key of child k at level l-1, which covers the
-// column range [k * span, (k + 1) * span) with span = W^l
-__global__ void k_gather_btree_level(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint64_t slots,
-                                     uint64_t* __restrict__ level) {
+// B+tree level l, W separators per node, fanout F = W + 1: slot k = (node j,
+// separator c) is the max key of child j*F + c one level down, which covers
+// the column range [child * span, (child + 1) * span); UINT64_MAX past the end
+__global__ void k_gather_btree_level(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint32_t W,
+                                     uint64_t slots, uint64_t* __restrict__ level) {
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < slots; k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t first = k * span;
+        const uint64_t child = (k / W) * (W + 1) + (k % W);
+        const uint64_t first = child * span;
         if (first < n) {
             uint64_t last = first + span;
             if (last > n) last = n;
@@ -108,6 +110,8 @@ int device_alloc(gj_index* idx, size_t bytes, void** out) {
     return GJ_OK;
 }
 
+uint32_t aligned32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31u) == 0 ? 1u : 0u; }
+
 int host_copy_of_column(const uint64_t* d_keys, const uint64_t* h_keys, uint64_t n, std::vector<uint64_t>* store,
                         const uint64_t** out) {
     if (h_keys) {
@@ -123,6 +127,7 @@ int host_copy_of_column(const uint64_t* d_keys, const uint64_t* h_keys, uint64_t
 int build_binary_search(gj_index* idx, cudaStream_t s) {
     idx->bs.col = idx->d_col;
     idx->bs.n = idx->n;
+    idx->bs.col_aligned = aligned32(idx->d_col);
     const uint32_t want = idx->params.bs_cache_keys;
     if (want == 0 || idx->n < 64) return GJ_OK;
     // slots: a power of two <= want; stride 2^shift with slots * 2^shift >= n
@@ -148,26 +153,24 @@ int build_binary_search(gj_index* idx, cudaStream_t s) {
 
 int build_btree(gj_index* idx, cudaStream_t s) {
     const uint32_t W = idx->params.btree_node_keys;
-    uint32_t logw = 0;
-    while ((1u << logw) < W) ++logw;
-    if ((1u << logw) != W || logw < 4 || logw > 6) {
-        set_error("btree: node size must be 16, 32 or 64 keys (got %u)", W);
+    const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 16;
+    if (!(W == 4 || W == 8 || W == 16 || W == 32 || W == 64) || L == 0 || L > 4096 || (L & (L - 1)) != 0) {
+        set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 8, 16, 32 or 64 separators, "
+                  "leaves of a power of two up to 4096 keys)", W, L);
         return GJ_ERR_INVALID_ARGUMENT;
     }
     const uint64_t n = idx->n;
-    // level sizes: level l has ceil(n / W^(l+1)) nodes; stop at one node
-    std::vector<uint64_t> nodes(1, 0);
-    uint64_t span = W;  // keys below one slot of level 1
+    const uint64_t F = (uint64_t)W + 1;
+    // level sizes: level l has ceil(nodes[l-1] / F) nodes; nodes[0] = leaves
+    std::vector<uint64_t> nodes(1, (n + L - 1) / L);
     for (int l = 1;; ++l) {
         if (l >= kBtreeMaxLevels) {
             set_error("btree: more than %d levels", kBtreeMaxLevels - 1);
             return GJ_ERR_UNSUPPORTED;
         }
-        const uint64_t node_span = span * W;  // keys below one node
-        const uint64_t cnt = (n + node_span - 1) / node_span;
+        const uint64_t cnt = (nodes[l - 1] + F - 1) / F;
         nodes.push_back(cnt);
         if (cnt == 1) break;
-        span = node_span;
     }
     const uint32_t height = (uint32_t)nodes.size() - 1;
     // storage: top level first so that the shared-memory cache is a prefix
@@ -180,14 +183,14 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     void* p = nullptr;
     GJ_TRY(device_alloc(idx, total * sizeof(uint64_t), &p));
     uint64_t* base = static_cast<uint64_t*>(p);
-    span = W;
+    uint64_t span = L;  // column keys below one child of a level-1 node
     for (uint32_t l = 1; l <= height; ++l) {
         const uint64_t slots = nodes[l] * W;
         const int grid = (int)std::min<uint64_t>((slots + 255) / 256, 65535);
-        k_gather_btree_level<<<grid, 256, 0, s>>>(idx->d_col, n, span, slots, base + offset[l]);
+        k_gather_btree_level<<<grid, 256, 0, s>>>(idx->d_col, n, span, W, slots, base + offset[l]);
         GJ_CUDA_TRY(cudaGetLastError());
         idx->bt.level[l] = base + offset[l];
-        span *= W;
+        span *= F;
     }
     // shared-memory cache: as many top levels as fit the budget
     uint32_t cached = 0;
@@ -205,7 +208,8 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     idx->bt.cached_levels = cached;
     idx->bt.cache_keys = (uint32_t)cache_keys;
     idx->bt.node_keys = W;
-    idx->bt_logw = logw;
+    idx->bt.leaf_keys = L;
+    idx->bt.col_aligned = aligned32(idx->d_col);
     uint64_t maxk = 0;
     GJ_CUDA_TRY(cudaMemcpyAsync(&maxk, idx->d_col + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -249,6 +253,7 @@ int build_harmonia(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
     }
     idx->hm.cached_nodes = (uint32_t)cached;
     idx->hm.cached_levels = cached_levels;
+    idx->hm.col_aligned = aligned32(idx->d_col);
     idx->bytes = (ha.keys.size() + ha.children.size()) * sizeof(uint64_t);
     return GJ_OK;
 }
@@ -276,6 +281,7 @@ int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t
     idx->rs.max_key = rs.max_key;
     idx->rs.shift = rs.shift;
     idx->rs.max_error = idx->params.rs_max_error;
+    idx->rs.col_aligned = aligned32(idx->d_col);
     idx->bytes = rs.table.size() * sizeof(uint32_t) + rs.sx.size() * (sizeof(uint64_t) + sizeof(double));
     return GJ_OK;
 }
@@ -286,6 +292,7 @@ int build_learned(gj_index* idx, cudaStream_t s);  // gj_learned.cu
 
 // owned allocation of an index (released by gj_index_free)
 int device_alloc_for(gj_index* idx, size_t bytes, void** out) { return device_alloc(idx, bytes, out); }
+uint32_t column_aligned32(const void* p) { return aligned32(p); }
 
 }  // namespace gj
 
@@ -304,7 +311,8 @@ void gj_index_params_default(gj_index_params* p) {
     if (!p) return;
     std::memset(p, 0, sizeof(*p));
     p->struct_size = sizeof(gj_index_params);
-    p->btree_node_keys = 64;
+    p->btree_node_keys = 4;
+    p->btree_leaf_keys = 16;
     p->rs_radix_bits = 18;
     p->rs_max_error = 32;
     p->bs_cache_keys = 4096;
@@ -456,6 +464,36 @@ int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* m
     if (max_error) *max_error = index->learned_max_error;
     if (mean_window) *mean_window = index->learned_mean_window;
     return GJ_OK;
+}
+
+int gj_index_device_view(const gj_index* index, void* view, size_t view_bytes) {
+    GJ_CHECK_ARG(index, "gj_index_device_view: null index");
+    auto copy = [&](const void* src, size_t bytes) -> int {
+        if (view_bytes != bytes || (bytes && !view)) {
+            set_error("gj_index_device_view: view_bytes %zu does not match the %zu-byte view of this index kind",
+                      view_bytes, bytes);
+            return GJ_ERR_INVALID_ARGUMENT;
+        }
+        if (bytes) std::memcpy(view, src, bytes);
+        return GJ_OK;
+    };
+    switch (index->type) {
+        case GJ_INDEX_BINARY_SEARCH: return copy(&index->bs, sizeof(index->bs));  // its fence lives in global memory
+        case GJ_INDEX_BTREE: {
+            gj::btree_view v = index->bt;
+            v.cached_levels = 0;
+            return copy(&v, sizeof(v));
+        }
+        case GJ_INDEX_HARMONIA: {
+            gj::harmonia_view v = index->hm;
+            v.cached_nodes = 0;
+            v.cached_levels = 0;
+            return copy(&v, sizeof(v));
+        }
+        case GJ_INDEX_RADIX_SPLINE: return copy(&index->rs, sizeof(index->rs));
+        case GJ_INDEX_LEARNED: return copy(&index->ln, sizeof(index->ln));
+        default: return copy(nullptr, 0);
+    }
 }
 
 int gj_index_lookup(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,

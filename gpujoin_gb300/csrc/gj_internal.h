@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "gpujoin.h"
@@ -108,7 +109,6 @@ struct gj_index {
 
     gj::bs_view bs{};
     gj::btree_view bt{};
-    uint32_t bt_logw = 6;
     gj::harmonia_view hm{};
     gj::rs_view rs{};
     gj::learned_view ln{};
@@ -136,6 +136,23 @@ int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, 
 size_t scan_workspace_bytes(uint64_t n);
 int inclusive_scan_sum(uint64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
 int inclusive_scan_max_signed(int64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
+
+// B+tree variants compiled: W in {4, 8, 16, 32, 64} separators per node;
+// fn receives std::integral_constant<int, W>
+template <class Fn>
+int btree_dispatch(uint32_t w, Fn&& fn) {
+    using std::integral_constant;
+    switch (w) {
+        case 4: return fn(integral_constant<int, 4>{});
+        case 8: return fn(integral_constant<int, 8>{});
+        case 16: return fn(integral_constant<int, 16>{});
+        case 32: return fn(integral_constant<int, 32>{});
+        case 64: return fn(integral_constant<int, 64>{});
+        default:
+            set_error("btree: unsupported node width %u", w);
+            return GJ_ERR_UNSUPPORTED;
+    }
+}
 
 // counter-based hashing shared by the generators and the learned trainer
 __host__ __device__ inline uint64_t mix64(uint64_t x) {

@@ -118,17 +118,10 @@ __global__ void __launch_bounds__(kJoinBlock) k_star_join(const Lookup lookup, c
     }
 }
 
-struct join_btree6 {
+template <int W>
+struct join_btree {
     btree_view v;
-    __device__ __forceinline__ uint32_t operator()(uint64_t key) const { return btree_lookup<6>(v, nullptr, key); }
-};
-struct join_btree5 {
-    btree_view v;
-    __device__ __forceinline__ uint32_t operator()(uint64_t key) const { return btree_lookup<5>(v, nullptr, key); }
-};
-struct join_btree4 {
-    btree_view v;
-    __device__ __forceinline__ uint32_t operator()(uint64_t key) const { return btree_lookup<4>(v, nullptr, key); }
+    __device__ __forceinline__ uint32_t operator()(uint64_t key) const { return btree_lookup<W>(v, nullptr, key); }
 };
 struct join_harmonia {
     harmonia_view v;
@@ -186,9 +179,10 @@ extern "C" int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk,
     hm.cached_levels = 0;
     switch (idx->type) {
         case GJ_INDEX_BTREE:
-            if (idx->bt_logw == 4) return run_star_join(join_btree4{bt}, idx, d_fk, d_date, d_price, d_discount, nfact, d_dim_flag, lo, hi, d_out, s);
-            if (idx->bt_logw == 5) return run_star_join(join_btree5{bt}, idx, d_fk, d_date, d_price, d_discount, nfact, d_dim_flag, lo, hi, d_out, s);
-            return run_star_join(join_btree6{bt}, idx, d_fk, d_date, d_price, d_discount, nfact, d_dim_flag, lo, hi, d_out, s);
+            return btree_dispatch(idx->bt.node_keys, [&](auto w) {
+                return run_star_join(join_btree<decltype(w)::value>{bt}, idx, d_fk, d_date, d_price, d_discount,
+                                     nfact, d_dim_flag, lo, hi, d_out, s);
+            });
         case GJ_INDEX_HARMONIA:
             return run_star_join(join_harmonia{hm}, idx, d_fk, d_date, d_price, d_discount, nfact, d_dim_flag, lo, hi, d_out, s);
         case GJ_INDEX_BINARY_SEARCH:

@@ -27,6 +27,7 @@
 namespace gj {
 
 int device_alloc_for(gj_index* idx, size_t bytes, void** out);  // gj_index.cu
+uint32_t column_aligned32(const void* p);                        // gj_index.cu
 
 namespace {
 
@@ -388,6 +389,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     v.num_leaves = L;
     v.root_kind = p.learned_root;
     v.hidden = H;
+    v.col_aligned = column_aligned32(idx->d_col);
 
     const uint32_t np = p.learned_root == GJ_LEARNED_ROOT_MLP ? mlp_param_count(H) : 2;
     const uint32_t np_padded = (np + 1) & ~1u;  // staged as 64-bit words

@@ -40,20 +40,12 @@ struct op_bs {
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return bs_lookup(v, cache, key);
     }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
-        bs_lookup_batch<K>(v, cache, key, res);
-    }
 };
-template <int LOGW>
+template <int W>
 struct op_btree {
     btree_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
-        return btree_lookup<LOGW>(v, cache, key);
-    }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
-        btree_lookup_batch<LOGW, K>(v, cache, key, res);
+        return btree_lookup<W>(v, cache, key);
     }
 };
 struct op_harmonia {
@@ -61,37 +53,30 @@ struct op_harmonia {
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return harmonia_lookup(v, cache, key);
     }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
-        harmonia_lookup_batch<K>(v, cache, key, res);
-    }
 };
 struct op_rs {
     rs_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const { return rs_lookup(v, key); }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t*, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
-        rs_lookup_batch<K>(v, key, res);
-    }
 };
 struct op_noop {
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t*, const uint64_t (&)[K], uint32_t (&res)[K]) const {
-#pragma unroll
-        for (int k = 0; k < K; ++k) res[k] = kInvalid;
-    }
 };
 struct op_learned {
     learned_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return learned_lookup(v, reinterpret_cast<const float*>(cache), key);
     }
-    template <int K>
-    __device__ __forceinline__ void batch(const uint64_t* cache, const uint64_t (&key)[K], uint32_t (&res)[K]) const {
-        learned_lookup_batch<K>(v, reinterpret_cast<const float*>(cache), key, res);
-    }
 };
+
+// the items of a thread are searched one after another: a search is a
+// chain of dependent loads, and occupancy (not per-thread interleaving)
+// keeps the loads of many probes in flight
+template <class Op, int K>
+__device__ __forceinline__ void run_items(const Op& op, const uint64_t* cache, const uint64_t (&key)[K],
+                                          uint32_t (&res)[K]) {
+#pragma unroll 1
+    for (int k = 0; k < K; ++k) res[k] = op(cache, key[k]);
+}
 
 __device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd) {
     for (uint32_t i = threadIdx.x; i < sd.words0; i += blockDim.x) dst[i] = __ldg(reinterpret_cast<const unsigned long long*>(sd.src0) + i);
@@ -126,7 +111,7 @@ __global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_lookup(const Op op, c
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
             key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
         }
-        op.template batch<kLookupItems>(cache, key, res);
+        run_items<Op, kLookupItems>(op, cache, key, res);
 #pragma unroll
         for (int k = 0; k < kLookupItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
@@ -152,7 +137,7 @@ __global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_scatter_lookup(const 
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
             key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(keys + i)) : 0ull;
         }
-        op.template batch<kLookupItems>(cache, key, res);
+        run_items<Op, kLookupItems>(op, cache, key, res);
 #pragma unroll
         for (int k = 0; k < kLookupItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
@@ -218,7 +203,7 @@ __global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_pairs(const Op op, co
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
             key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
         }
-        op.template batch<kItems>(cache, key, pos);
+        run_items<Op, kItems>(op, cache, key, pos);
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
@@ -410,11 +395,7 @@ int with_op(const gj_index* idx, Fn&& fn) {
     switch (idx->type) {
         case GJ_INDEX_BINARY_SEARCH: return fn(op_bs{idx->bs});
         case GJ_INDEX_BTREE:
-            switch (idx->bt_logw) {
-                case 4: return fn(op_btree<4>{idx->bt});
-                case 5: return fn(op_btree<5>{idx->bt});
-                default: return fn(op_btree<6>{idx->bt});
-            }
+            return btree_dispatch(idx->bt.node_keys, [&](auto w) { return fn(op_btree<decltype(w)::value>{idx->bt}); });
         case GJ_INDEX_HARMONIA: return fn(op_harmonia{idx->hm});
         case GJ_INDEX_RADIX_SPLINE: return fn(op_rs{idx->rs});
         case GJ_INDEX_LEARNED: return fn(op_learned{idx->ln});

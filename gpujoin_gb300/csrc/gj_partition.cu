@@ -56,27 +56,23 @@ __global__ void k_part_offsets(const uint64_t* __restrict__ incl, uint32_t fanou
         offsets[p] = p == 0 ? 0 : (p == fanout ? m : incl[(uint64_t)p * nblocks - 1]);
 }
 
-// scatter block b's chunk; the running offsets start at the exclusive
-// prefix of (p, b).  Ranks inside a block come from shared-memory atomics,
-// so the order inside a partition follows the block order but not the probe
-// order within one block.
+// scatter block b's chunk.  The flat (partition, block) order of the scanned
+// histogram makes the start of cell c the inclusive sum of cell c - 1, so the
+// keys are read once.  Ranks inside a block come from shared-memory atomics:
+// the order inside a partition follows the block order, not the probe order
+// within one block.
 __global__ void __launch_bounds__(kPartBlock) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
                                                              uint64_t chunk, uint64_t min_key, uint32_t shift,
                                                              uint32_t fanout, const uint64_t* __restrict__ incl,
                                                              uint64_t row_base, uint64_t* __restrict__ out_keys,
                                                              uint32_t* __restrict__ out_rows) {
     extern __shared__ unsigned long long s_next[];
-    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_next + fanout);
-    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_cnt[p] = 0;
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) {
+        const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
+        s_next[p] = cell == 0 ? 0ull : incl[cell - 1];
+    }
     __syncthreads();
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
-    // this block's own counts, to turn the inclusive scan into its start offsets
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-        atomicAdd(&s_cnt[part_of(__ldg(reinterpret_cast<const unsigned long long*>(keys) + i), min_key, shift, fanout)], 1u);
-    __syncthreads();
-    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x)
-        s_next[p] = incl[(uint64_t)p * gridDim.x + blockIdx.x] - s_cnt[p];
-    __syncthreads();
     for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
         const uint64_t k = __ldcs(reinterpret_cast<const unsigned long long*>(keys) + i);
         const uint32_t p = part_of(k, min_key, shift, fanout);
@@ -129,7 +125,7 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
         return GJ_OK;
     }
     const size_t smem_hist = pl.fanout * sizeof(uint32_t);
-    const size_t smem_scatter = pl.fanout * (sizeof(unsigned long long) + sizeof(uint32_t));
+    const size_t smem_scatter = pl.fanout * sizeof(unsigned long long);
     if (smem_scatter > 48 * 1024)
         GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_scatter));
     k_part_hist<<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);

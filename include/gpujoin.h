@@ -65,7 +65,9 @@ typedef enum gj_index_type {
  * (src/indexes.cuh:88-91,169-174,329-334; src/index_lookup_config.hpp:18-37). */
 typedef struct gj_index_params {
     uint32_t struct_size;       /* = sizeof(gj_index_params) */
-    uint32_t btree_node_keys;   /* keys per B+tree node: 16, 32 or 64 (default 64) */
+    uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout + 1): 4, 8, 16, 32 or 64 (default 4:
+                                   one 32-byte sector per node) */
+    uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 16) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */
     uint32_t rs_max_error;      /* RadixSpline spline error (default 32) */
     uint32_t bs_cache_keys;     /* binary search: sampled keys staged in shared memory (default 4096, 0 = off) */
@@ -112,6 +114,15 @@ uint64_t gj_index_size(const gj_index* index);
  * search-window width over the build keys */
 int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* mean_window);
 
+/* The index's device view -- the struct passed by value to kernels, like
+ * the reference's device_index_t member (src/indexes.cuh:18-22,116-124) --
+ * for kernels written against include/gpujoin/device.cuh.  view_bytes must
+ * equal the size of the view of the index kind (gj::bs_view, btree_view,
+ * harmonia_view, rs_view, learned_view; 0 for no_op).  The view does not
+ * use the shared-memory caches of the library's own kernels.  Valid while
+ * the index lives. */
+int gj_index_device_view(const gj_index* index, void* view, size_t view_bytes);
+
 /* Plain INLJ probe, lookup_kernel (src/index_lookup_common.cuh:217-245):
  * d_positions[i] = device_index_t::cooperative_lookup(d_probes[i]) with the
  * reference's per-index result semantics:
@@ -153,9 +164,10 @@ int gj_inlj_pairs_noalloc(const gj_index* index, const uint64_t* d_probes, uint6
  * + gpu_chunked_laswwc_radix_partition_int64_int64 as called from
  * run_on_stream (src/index_lookup_partitioning.cu:300-359).  Partition of a
  * key = min(((key - min_key) >> shift), 2^radix_bits - 1), keys <= min_key in
- * partition 0.  Output is stable (probe order within a partition):
- * d_out_keys / d_out_rows hold m entries, d_offsets 2^radix_bits + 1.
- * radix_bits in [1, 12]. */
+ * partition 0.  Partitions follow each other in key order; inside a
+ * partition the tuples of earlier probe chunks come first, the order within
+ * one chunk is not fixed.  d_out_keys / d_out_rows hold m entries, d_offsets
+ * 2^radix_bits + 1.  radix_bits in [1, 12]. */
 int gj_partition_workspace_size(uint64_t m, uint32_t radix_bits, size_t* bytes);
 int gj_range_partition(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift,
                        uint32_t radix_bits, uint64_t* d_out_keys, uint32_t* d_out_rows,

@@ -1,0 +1,64 @@
+// A probe written the way the reference's code is written -- index class
+// templates, construct(h_column, d_column), a kernel taking the index's
+// device_index by value and calling cooperative_lookup(active, key) -- built
+// against include/gpujoin/indexes.cuh and libgpujoin.so.  Used by
+// tests/test_drop_in.py to show that such code compiles and probes
+// correctly without changes to its structure.
+#include <cstdint>
+#include <exception>
+#include <vector>
+
+#include "gpujoin/indexes.cuh"
+
+using index_key_t = uint64_t;
+using value_t = uint64_t;
+
+template <class IndexStructureType>
+__global__ void probe_all(const IndexStructureType index_structure, uint64_t n, const index_key_t* __restrict__ keys,
+                          value_t* __restrict__ tids) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // the loop bound is rounded up to whole warps so every lane reaches the lookup
+    const uint64_t limit = (n + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < limit; i += stride) {
+        const bool active = i < n;
+        const index_key_t key = active ? keys[i] : 0;
+        const value_t tid = index_structure.cooperative_lookup(active, key);
+        if (active) tids[i] = tid;
+    }
+}
+
+template <class IndexType>
+static int run(const index_key_t* d_col, const index_key_t* h_col, uint64_t n, const index_key_t* d_keys,
+               uint64_t m, value_t* d_tids) {
+    IndexType index;
+    index.construct(vector_view<index_key_t>(const_cast<index_key_t*>(h_col), n), d_col);
+    const int block = 128;
+    const uint64_t blocks = (m + block - 1) / block;
+    probe_all<<<(unsigned)(blocks ? (blocks < 65535 ? blocks : 65535) : 1), block>>>(index.device_index, m, d_keys,
+                                                                                     d_tids);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : 2;
+}
+
+extern "C" int drop_in_probe(int kind, const index_key_t* d_col, const index_key_t* h_col, uint64_t n,
+                             const index_key_t* d_keys, uint64_t m, value_t* d_tids) {
+    try {
+        switch (parse_index_type(kind == 0 ? "btree" : kind == 1 ? "harmonia" : kind == 2 ? "binary_search"
+                                 : kind == 3 ? "radix_spline" : kind == 4 ? "no_op" : "learned")) {
+            case index_type_enum::btree: return run<btree_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+            case index_type_enum::harmonia:
+                return run<harmonia_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+            case index_type_enum::binary_search:
+                return run<binary_search_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+            case index_type_enum::radix_spline:
+                return run<radix_spline_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+            case index_type_enum::no_op: return run<no_op_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+            case index_type_enum::learned:
+                return run<learned_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, d_tids);
+        }
+    } catch (const std::exception&) {
+        return 1;
+    }
+    return 3;
+}
+
+extern "C" const char* drop_in_type_name() { return type_name<btree_index<index_key_t, value_t>>::value(); }

@@ -73,17 +73,37 @@ def test_lookup_small_ragged_sizes(orc, gj, cuda, kind, n):
     np.testing.assert_array_equal(got, expected(orc, kind, col, pr))
 
 
-@pytest.mark.parametrize("node_keys", [16, 32, 64])
-def test_btree_node_widths(orc, gj, cuda, node_keys):
+@pytest.mark.parametrize("node_keys,leaf_keys", [(4, 4), (4, 16), (4, 64), (8, 8), (8, 16), (16, 16), (32, 16),
+                                                  (64, 16), (64, 64), (4, 1), (16, 2), (64, 256)])
+def test_btree_node_widths(orc, gj, cuda, node_keys, leaf_keys):
     import torch
 
-    rng = np.random.default_rng(node_keys)
-    for n in (1, node_keys - 1, node_keys, node_keys + 1, node_keys ** 2 + 3, 123457):
+    rng = np.random.default_rng(node_keys * 100 + leaf_keys)
+    for n in sorted({max(1, x) for x in (1, leaf_keys - 1, leaf_keys, leaf_keys + 1, node_keys * leaf_keys + 3, 123457)}):
         col = column(rng, n)
         pr = probes_for(rng, col, 3000)
-        ix = gj.btree_index(btree_node_keys=node_keys).construct(None, to_dev(torch, col))
+        ix = gj.btree_index(btree_node_keys=node_keys, btree_leaf_keys=leaf_keys).construct(None, to_dev(torch, col))
         got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
-        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"W={node_keys} n={n}")
+        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"W={node_keys} L={leaf_keys} n={n}")
+
+
+def test_unaligned_column(orc, gj, cuda):
+    # columns that start 8 and 16 bytes into an allocation: 32-byte sector loads must not be used
+    import torch
+
+    rng = np.random.default_rng(8)
+    col = column(rng, 32 * 3000)
+    pr = to_dev(torch, probes_for(rng, col, 5000))
+    h_pr = pr.cpu().numpy().view(np.uint64)
+    for shift in (1, 2):
+        buf = torch.zeros(len(col) + shift, dtype=torch.int64, device="cuda")
+        buf[shift:] = to_dev(torch, col)
+        d_col = buf[shift:]
+        assert d_col.data_ptr() % 32 == 8 * shift
+        for kind in ("btree", "harmonia", "binary_search", "radix_spline", "learned"):
+            ix = gj.make_index(kind).construct(None, d_col)
+            exp = orc.exact_lookup(col, h_pr) if kind in ("btree", "harmonia") else orc.bs_lookup(col, h_pr)
+            np.testing.assert_array_equal(from_dev_u32(ix.lookup(pr)), exp, err_msg=f"{kind} shift {shift}")
 
 
 @pytest.mark.parametrize("cache_keys", [0, 2, 64, 4096])
@@ -171,6 +191,9 @@ def test_build_errors(gj, cuda):
     assert e.value.code == 1
     with pytest.raises(gj.GJError):
         gj.btree_index(btree_node_keys=48).construct(None, torch.arange(0, 100, dtype=torch.int64, device="cuda"))
+    with pytest.raises(gj.GJError):
+        gj.btree_index(btree_node_keys=64, btree_leaf_keys=24).construct(
+            None, torch.arange(0, 100, dtype=torch.int64, device="cuda"))
     with pytest.raises(gj.GJError):
         gj.btree_index().construct(None, torch.empty(0, dtype=torch.int64, device="cuda"))
 
