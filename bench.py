@@ -302,14 +302,28 @@ def inlj_workload(args, world, rank, device, stream):
         e2e = {"value": world * m * e_steps / (e_ms / 1e3), "unit": "probe tuples/s", "h2d_bytes_per_step": 8 * m,
                "d2h_bytes_per_step": 8 * m}
 
+    # Roofline of the dominant kernel.  A pairs step is two launches: the
+    # search pass (k_lookup: probe key in, one 32-byte leaf sector, u32
+    # position out to the upper half of the pairs buffer) and the ordered
+    # compaction (u32 in, 8-byte pair out).  The search pass is timed on its
+    # own here -- the same kernel on the same probes and output location, CUDA
+    # events on the same stream; its algorithmic bytes are 8 + 32 + 4 per probe.
     peak, peak_kind = measured_peak()
-    per_launch_ms = headline_ms / args.steps
-    achieved = bytes_per_probe * m / (per_launch_ms / 1e3) / 1e9
-    traffic = profile_traffic(f"inlj_pairs_{headline_index}_n{args.n_log2}_m{args.m_log2}")
+    lookup_bytes_per_probe = bytes_per_probe - 4
+    lookup_ms = time_steps(lambda: headline_ix.lookup(probes, out=pairs[m:]), args.steps, args.warmup, stream, world,
+                           device)
+    lookup_ms = max_over_ranks(lookup_ms, world, device) / args.steps
+    achieved = lookup_bytes_per_probe * m / (lookup_ms / 1e3) / 1e9
+    traffic = profile_traffic(f"k_lookup_{headline_index}_n{args.n_log2}_m{args.m_log2}")
+    step_ms = headline_ms / args.steps
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} hbm_gbs (copy, burst)",
-                "bytes_per_probe": bytes_per_probe}
+                "kernel": f"k_lookup<{headline_index}> (search pass of the pairs step)",
+                "kernel_ms": round(lookup_ms, 4), "kernel_share_of_step": round(lookup_ms / step_ms, 3),
+                "bytes_per_probe": lookup_bytes_per_probe,
+                "step_bytes_per_probe": bytes_per_probe,
+                "step_achieved": round(bytes_per_probe * m / (step_ms / 1e3) / 1e9, 1)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -340,7 +354,7 @@ def inlj_workload(args, world, rank, device, stream):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
     return line

@@ -105,6 +105,7 @@ _SIGNATURES = {
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_inlj_pairs_status": (_i32, [_vp, _sz, _u64, _vp]),
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
@@ -280,6 +281,12 @@ class abstract_index:
         _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
                                    _ptr(workspace), workspace.numel(), _stream(stream)))
         return out_pairs, out_count
+
+    @staticmethod
+    def inlj_pairs_status(workspace, m: int, stream=None) -> None:
+        """Raise GJError (GJ_ERR_TIMEOUT) if the last inlj_pairs on this
+        workspace gave up a bounded wait; synchronises the stream."""
+        _check(lib().gj_inlj_pairs_status(_ptr(workspace), workspace.numel(), m, _stream(stream)))
 
     def inlj_pairs_noalloc(self, d_probes, out_pairs, out_count, stream=None):
         """inlj_pairs without a workspace: the scratch is a fixed array inside the

@@ -153,7 +153,7 @@ int build_binary_search(gj_index* idx, cudaStream_t s) {
 
 int build_btree(gj_index* idx, cudaStream_t s) {
     const uint32_t W = idx->params.btree_node_keys;
-    const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 16;
+    const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 8;
     if (!(W == 4 || W == 8 || W == 16 || W == 32 || W == 64) || L == 0 || L > 4096 || (L & (L - 1)) != 0) {
         set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 8, 16, 32 or 64 separators, "
                   "leaves of a power of two up to 4096 keys)", W, L);
@@ -312,7 +312,7 @@ void gj_index_params_default(gj_index_params* p) {
     std::memset(p, 0, sizeof(*p));
     p->struct_size = sizeof(gj_index_params);
     p->btree_node_keys = 4;
-    p->btree_leaf_keys = 16;
+    p->btree_leaf_keys = 8;
     p->rs_radix_bits = 18;
     p->rs_max_error = 32;
     p->bs_cache_keys = 4096;
@@ -519,6 +519,17 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
     }
     return launch_pairs(index, d_probes, m, nullptr, d_pairs, nullptr, d_count, d_workspace, workspace_bytes,
                         as_stream(stream));
+}
+
+int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream) {
+    GJ_CHECK_ARG(d_workspace, "gj_inlj_pairs_status: null workspace");
+    unsigned int flag = 0;
+    GJ_TRY(pairs_error_flag(const_cast<void*>(d_workspace), workspace_bytes, m, &flag, as_stream(stream)));
+    if (flag) {
+        set_error("inlj pairs: a tile waited too long for its predecessors' counts; the pairs are incomplete");
+        return GJ_ERR_TIMEOUT;
+    }
+    return GJ_OK;
 }
 
 }  // extern "C"

@@ -20,9 +20,16 @@ namespace gj {
 namespace {
 
 constexpr int kBlock = 256;
-// resident blocks per SM the lookup kernels are compiled for (register cap)
-#ifndef GJ_MIN_BLOCKS
-#define GJ_MIN_BLOCKS 1
+// Resident blocks per SM each lookup kernel is compiled for: the register
+// cap.  A search is a chain of dependent loads and the warps of an SM are
+// what keeps loads in flight, so the tree and search kinds are capped at 32
+// registers (8 blocks of 256 threads, full occupancy), which they meet
+// without spilling; the learned index keeps 64 for its MLP root.
+// GJ_MIN_BLOCKS overrides every kind (tuning builds).
+#ifdef GJ_MIN_BLOCKS
+#define GJ_BLOCKS(n) GJ_MIN_BLOCKS
+#else
+#define GJ_BLOCKS(n) (n)
 #endif
 
 // ---------------------------------------------------------------------------
@@ -36,6 +43,7 @@ struct stage_desc {
 };
 
 struct op_bs {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
     bs_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return bs_lookup(v, cache, key);
@@ -43,40 +51,35 @@ struct op_bs {
 };
 template <int W>
 struct op_btree {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
     btree_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return btree_lookup<W>(v, cache, key);
     }
 };
 struct op_harmonia {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
     harmonia_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return harmonia_lookup(v, cache, key);
     }
 };
 struct op_rs {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
     rs_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const { return rs_lookup(v, key); }
 };
 struct op_noop {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
 };
 struct op_learned {
+    static constexpr int kMinBlocks = GJ_BLOCKS(4);
     learned_view v;
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
         return learned_lookup(v, reinterpret_cast<const float*>(cache), key);
     }
 };
-
-// the items of a thread are searched one after another: a search is a
-// chain of dependent loads, and occupancy (not per-thread interleaving)
-// keeps the loads of many probes in flight
-template <class Op, int K>
-__device__ __forceinline__ void run_items(const Op& op, const uint64_t* cache, const uint64_t (&key)[K],
-                                          uint32_t (&res)[K]) {
-#pragma unroll 1
-    for (int k = 0; k < K; ++k) res[k] = op(cache, key[k]);
-}
 
 __device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd) {
     for (uint32_t i = threadIdx.x; i < sd.words0; i += blockDim.x) dst[i] = __ldg(reinterpret_cast<const unsigned long long*>(sd.src0) + i);
@@ -88,74 +91,82 @@ __device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd)
 // ---------------------------------------------------------------------------
 // plain lookup: out[i] = lookup(probes[i])
 // ---------------------------------------------------------------------------
-// A block processes tiles of kLookupItems * kBlock probes; item k of thread t
-// is probe tile + k * kBlock + t (coalesced), and the kLookupItems probes of a
-// thread are searched in lockstep.
+// One block per tile of kLookupItems * kBlock probes (item k of thread t is
+// probe tile + k * kBlock + t: coalesced).  The grid is not persistent: the
+// hardware hands tiles to SMs as they free up, which balances SMs that run
+// at different speeds (near and far HBM of the two dies) without a counter.
+// A thread searches its probes one after another (a search is a chain of
+// dependent loads; occupancy, not per-thread interleaving, keeps many loads
+// in flight) and loads the next probe key before it searches the current
+// one.  No per-thread arrays: the search runs with few live registers.
 #ifndef GJ_LOOKUP_ITEMS
 #define GJ_LOOKUP_ITEMS 8
 #endif
 constexpr int kLookupItems = GJ_LOOKUP_ITEMS;
+constexpr uint32_t kLookupTile = kBlock * kLookupItems;
+
+__device__ __forceinline__ uint64_t load_probe(const uint64_t* p, uint64_t i, uint64_t m) {
+    return i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(p + i)) : 0ull;
+}
 
 template <class Op>
-__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_lookup(const Op op, const stage_desc sd,
                                                    const uint64_t* __restrict__ probes, uint64_t m,
                                                    uint32_t* __restrict__ out) {
     extern __shared__ uint64_t cache[];
     stage_cache(cache, sd);
-    constexpr uint64_t tile = (uint64_t)kLookupItems * kBlock;
-    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < m; t0 += (uint64_t)gridDim.x * tile) {
-        uint64_t key[kLookupItems];
-        uint32_t res[kLookupItems];
-#pragma unroll
-        for (int k = 0; k < kLookupItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
-        }
-        run_items<Op, kLookupItems>(op, cache, key, res);
-#pragma unroll
-        for (int k = 0; k < kLookupItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            if (i < m) __stcs(out + i, res[k]);
-        }
+    const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
+    uint64_t next = load_probe(probes, t0, m);
+#pragma unroll 1
+    for (int k = 0; k < kLookupItems; ++k) {
+        const uint64_t i = t0 + (uint64_t)k * kBlock;
+        if (i >= m) break;
+        const uint64_t key = next;
+        if (k + 1 < kLookupItems) next = load_probe(probes, i + kBlock, m);
+        __stcs(out + i, op(cache, key));
     }
 }
 
 // scattered lookup over a partitioned relation: out[rows[i]] = lookup(keys[i])
 template <class Op>
-__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_scatter_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const Op op, const stage_desc sd,
                                                            const uint64_t* __restrict__ keys,
                                                            const uint32_t* __restrict__ rows, uint64_t m,
                                                            uint32_t* __restrict__ out) {
     extern __shared__ uint64_t cache[];
     stage_cache(cache, sd);
-    constexpr uint64_t tile = (uint64_t)kLookupItems * kBlock;
-    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < m; t0 += (uint64_t)gridDim.x * tile) {
-        uint64_t key[kLookupItems];
-        uint32_t res[kLookupItems];
-#pragma unroll
-        for (int k = 0; k < kLookupItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(keys + i)) : 0ull;
-        }
-        run_items<Op, kLookupItems>(op, cache, key, res);
-#pragma unroll
-        for (int k = 0; k < kLookupItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            if (i < m) out[__ldcs(rows + i)] = res[k];
-        }
+    const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
+    uint64_t next = load_probe(keys, t0, m);
+#pragma unroll 1
+    for (int k = 0; k < kLookupItems; ++k) {
+        const uint64_t i = t0 + (uint64_t)k * kBlock;
+        if (i >= m) break;
+        const uint64_t key = next;
+        if (k + 1 < kLookupItems) next = load_probe(keys, i + kBlock, m);
+        const uint32_t r = op(cache, key);
+        out[__ldcs(rows + i)] = r;
     }
 }
 
 // ---------------------------------------------------------------------------
 // join pairs with decoupled look-back compaction
 // ---------------------------------------------------------------------------
-// Tiles of kBlock * kItems probes are claimed in order through an atomic
-// counter, so every predecessor of a tile is already running when the tile
-// looks back: each wait ends.  Waits are bounded anyway; on expiry the kernel
-// raises the error flag (GJ_ERR_TIMEOUT on the host) and stops writing.
-constexpr int kItems = GJ_LOOKUP_ITEMS;
+// Pairs are emitted in probe order.  Tiles of kBlock * items probes are
+// claimed in order through an atomic counter, so every predecessor of a tile
+// is already running when the tile looks back: each wait ends.  Waits are
+// bounded anyway; on expiry the kernel raises the error flag (GJ_ERR_TIMEOUT
+// on the host) and stops writing.
+//
+// Plain probes take two passes: k_lookup writes the positions to the upper
+// half of the pairs buffer (the caller provides 2m u32), then
+// k_compact_pairs turns them into pairs.  The search pass has no block
+// barriers, and the compaction is a streaming pass.  Probes of a partitioned
+// relation (row ids, appended behind *d_base) take the single-pass k_pairs.
+constexpr int kItems = GJ_LOOKUP_ITEMS;          // k_pairs items per thread
+constexpr int kCompactItems = 16;                // k_compact_pairs items per thread
 static_assert(kItems >= 4 && (kItems & (kItems - 1)) == 0, "the pairs scan needs a power-of-two item count >= 4");
-constexpr uint32_t kTile = kBlock * kItems;
+constexpr uint32_t kTile = kBlock * kItems;      // also the workspace's tile unit (the larger tile count)
+constexpr uint32_t kCompactTile = kBlock * kCompactItems;
 constexpr unsigned long long kFlagAggregate = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
 constexpr unsigned long long kValueMask = (1ull << 62) - 1;
@@ -167,120 +178,189 @@ struct pairs_ws {
     unsigned int* error;             // 1
 };
 
+// Exclusive prefix of tile `tile` (> 0) from the states of its predecessors,
+// read 32 at a time by the calling warp: lane i reads tile j - i, and the
+// window is summed up to its nearest published prefix.  Returns false when
+// the wait ran out.
+__device__ __forceinline__ bool look_back(const pairs_ws& ws, uint32_t tile, uint32_t lane,
+                                          unsigned long long* prefix_out) {
+    unsigned long long prefix = 0;
+    int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    for (;;) {
+        const int64_t idx = j - (int64_t)lane;
+        const unsigned long long st =
+            idx >= 0 ? *reinterpret_cast<volatile unsigned long long*>(&ws.tile_state[idx]) : (kFlagPrefix | 0ull);
+        const unsigned long long flag = st & ~kValueMask;
+        const uint32_t not_ready = __ballot_sync(0xffffffffu, flag == 0);
+        const uint32_t has_prefix = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+        // lanes up to (and including) the nearest prefix must all be published
+        const uint32_t need = has_prefix ? (2u << (__ffs(has_prefix) - 1)) - 1u : 0xffffffffu;
+        if (not_ready & need) {
+            if (++spins > kSpinLimit) return false;
+            continue;
+        }
+        unsigned long long v = ((need >> lane) & 1u) ? (st & kValueMask) : 0ull;
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        prefix += v;
+        if (has_prefix) break;
+        j -= 32;
+    }
+    *prefix_out = prefix;
+    return true;
+}
+
+// One block-tile of the ordered compaction: fill(t0, s_pos) writes the
+// result of probe t0 + j into s_pos[j] (kInvalid for no pair) for the
+// tile's kBlock * kIt probes; the block then emits the pairs of the tile at
+// the tile's prefix.  Returns false when the kernel must stop (look-back
+// timed out).
+template <int kIt, class Fill>
+__device__ __forceinline__ bool pairs_tile(Fill&& fill, uint32_t tile, const uint32_t* __restrict__ rows, uint64_t m,
+                                           uint2* pairs, uint64_t base, uint64_t* __restrict__ d_count,
+                                           const pairs_ws& ws, uint32_t num_tiles) {
+    constexpr int kWarps = kBlock / 32;
+    constexpr uint32_t kT = kBlock * kIt;
+    __shared__ uint32_t s_cnt[kIt * kWarps];
+    __shared__ uint32_t s_ballot[kIt * kWarps];
+    __shared__ uint32_t s_pos[kT];
+    __shared__ unsigned long long s_prefix;
+    __shared__ int s_abort;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t t0 = (uint64_t)tile * kT;
+    // item k of thread t is probe t0 + k * kBlock + t; output order is probe
+    // order, i.e. (k, warp, lane) order
+    fill(t0, s_pos);
+    uint32_t flags = 0;
+#pragma unroll
+    for (int k = 0; k < kIt; ++k) {
+        const bool hit = s_pos[k * kBlock + threadIdx.x] != kInvalid;
+        const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
+        if (hit) flags |= 1u << k;
+        if (lane == 0) {
+            s_cnt[k * kWarps + warp] = __popc(ballot);
+            s_ballot[k * kWarps + warp] = ballot;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // exclusive scan of the kIt * kWarps counts in (k, warp) order
+        constexpr int kPerLane = kIt * kWarps / 32;
+        uint32_t v[kPerLane];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kPerLane; ++j) {
+            v[j] = s_cnt[lane * kPerLane + j];
+            sum += v[j];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += t;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int j = 0; j < kPerLane; ++j) {
+            s_cnt[lane * kPerLane + j] = run;
+            run += v[j];
+        }
+        // publish the tile aggregate, then resolve the tile prefix
+        const unsigned long long total = __shfl_sync(0xffffffffu, incl, 31);
+        unsigned long long prefix = 0;
+        bool ok = true;
+        if (tile == 0) {
+            if (lane == 0) atomicExch(&ws.tile_state[0], kFlagPrefix | total);
+        } else {
+            if (lane == 0) atomicExch(&ws.tile_state[tile], kFlagAggregate | total);
+            ok = look_back(ws, tile, lane, &prefix);
+            if (lane == 0) {
+                if (ok)
+                    atomicExch(&ws.tile_state[tile], kFlagPrefix | (prefix + total));
+                else
+                    atomicExch(ws.error, 1u);
+            }
+        }
+        if (lane == 0) {
+            s_abort = ok ? 0 : 1;
+            s_prefix = prefix;
+            if (ok && tile == num_tiles - 1) *d_count = base + prefix + total;
+        }
+    }
+    __syncthreads();
+    if (s_abort) return false;
+    const uint64_t tile_base = base + s_prefix;
+#pragma unroll
+    for (int k = 0; k < kIt; ++k) {
+        if (flags & (1u << k)) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            const uint32_t rank = __popc(s_ballot[k * kWarps + warp] & ((1u << lane) - 1u));
+            const uint64_t o = tile_base + s_cnt[k * kWarps + warp] + rank;
+            const uint32_t row = rows ? __ldcs(rows + i) : (uint32_t)i;
+            const uint32_t pos = s_pos[k * kBlock + threadIdx.x];
+            __stcs(reinterpret_cast<unsigned long long*>(pairs + o), ((unsigned long long)pos << 32) | row);
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+__device__ __forceinline__ uint32_t claim_tile(const pairs_ws& ws) {
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ws.tile_counter, 1u);
+    __syncthreads();
+    return s_tile;
+}
+
+// single pass: search and compact tile by tile (partitioned relations, whose
+// pairs are appended behind *d_base)
 template <class Op>
-__global__ void __launch_bounds__(kBlock, GJ_MIN_BLOCKS) k_pairs(const Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
                                                   const uint32_t* __restrict__ rows, uint64_t m,
                                                   uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
                                                   uint64_t* __restrict__ d_count, pairs_ws ws, uint32_t num_tiles) {
     extern __shared__ uint64_t cache[];
-    constexpr int kWarps = kBlock / 32;
-    __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_cnt[kItems * kWarps];
-    __shared__ unsigned long long s_prefix;
-    __shared__ int s_abort;
     stage_cache(cache, sd);
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t base = d_base ? *d_base : 0ull;
-
+    auto search = [&](uint64_t t0, uint32_t* s_pos) {
+        uint64_t next = load_probe(probes, t0 + threadIdx.x, m);
+#pragma unroll 1
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
+            const uint64_t key = next;
+            if (k + 1 < kItems) next = load_probe(probes, i + kBlock, m);
+            s_pos[k * kBlock + threadIdx.x] = i < m ? op(cache, key) : kInvalid;
+        }
+    };
     for (;;) {
-        if (threadIdx.x == 0) {
-            s_tile = atomicAdd(ws.tile_counter, 1u);
-            s_abort = 0;
-        }
-        __syncthreads();
-        const uint32_t tile = s_tile;
+        const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
-        const uint64_t t0 = (uint64_t)tile * kTile;
+        if (!pairs_tile<kItems>(search, tile, rows, m, pairs, base, d_count, ws, num_tiles)) break;
+    }
+}
 
-        // item k of thread t is probe t0 + k * kBlock + t: coalesced loads;
-        // output order is probe order, i.e. (k, warp, lane) order
-        uint32_t pos[kItems];
-        uint32_t lane_rank[kItems];
-        uint32_t flags = 0;
-        uint64_t key[kItems];
+// Second pass of the two-pass pairs: compact the positions k_lookup wrote
+// to the upper half of the pairs buffer (u32 index m + i) into pairs.  A
+// tile writes pairs only after every earlier tile has published its count,
+// i.e. after every earlier tile has read its positions, and pair o covers
+// u32 indices 2o and 2o+1 < m + i for the tile's own probes i >= o: no
+// position is overwritten before it is read.  (stash and pairs alias, so
+// neither is __restrict__.)
+__global__ void __launch_bounds__(kBlock) k_compact_pairs(const uint32_t* stash, uint64_t m, uint2* pairs,
+                                                          uint64_t* __restrict__ d_count, pairs_ws ws,
+                                                          uint32_t num_tiles) {
+    auto load = [&](uint64_t t0, uint32_t* s_pos) {
 #pragma unroll
-        for (int k = 0; k < kItems; ++k) {
+        for (int k = 0; k < kCompactItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            key[k] = i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + i)) : 0ull;
+            s_pos[k * kBlock + threadIdx.x] = i < m ? __ldcs(stash + i) : kInvalid;
         }
-        run_items<Op, kItems>(op, cache, key, pos);
-#pragma unroll
-        for (int k = 0; k < kItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            if (i >= m) pos[k] = kInvalid;
-            const bool hit = pos[k] != kInvalid;
-            const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
-            lane_rank[k] = __popc(ballot & ((1u << lane) - 1u));
-            if (hit) flags |= 1u << k;
-            if (lane == 0) s_cnt[k * kWarps + warp] = __popc(ballot);
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // exclusive scan of the kItems * kWarps counts in (k, warp) order
-            constexpr int kPerLane = kItems * kWarps / 32;
-            uint32_t v[kPerLane];
-            uint32_t sum = 0;
-#pragma unroll
-            for (int j = 0; j < kPerLane; ++j) {
-                v[j] = s_cnt[lane * kPerLane + j];
-                sum += v[j];
-            }
-            uint32_t incl = sum;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= (uint32_t)d) incl += t;
-            }
-            uint32_t run = incl - sum;
-#pragma unroll
-            for (int j = 0; j < kPerLane; ++j) {
-                s_cnt[lane * kPerLane + j] = run;
-                run += v[j];
-            }
-            if (lane == 31) {
-                // publish the tile aggregate, then resolve the tile prefix
-                const unsigned long long total = incl;
-                unsigned long long prefix = 0;
-                if (tile == 0) {
-                    atomicExch(&ws.tile_state[0], kFlagPrefix | total);
-                } else {
-                    atomicExch(&ws.tile_state[tile], kFlagAggregate | total);
-                    int64_t j = (int64_t)tile - 1;
-                    uint32_t spins = 0;
-                    while (j >= 0) {
-                        const unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(&ws.tile_state[j]);
-                        const unsigned long long flag = st & ~kValueMask;
-                        if (flag == 0) {
-                            if (++spins > kSpinLimit) {
-                                atomicExch(ws.error, 1u);
-                                s_abort = 1;
-                                break;
-                            }
-                            continue;
-                        }
-                        prefix += st & kValueMask;
-                        if (flag == kFlagPrefix) break;
-                        --j;
-                    }
-                    atomicExch(&ws.tile_state[tile], kFlagPrefix | (prefix + total));
-                }
-                s_prefix = prefix;
-                if (tile == num_tiles - 1) *d_count = base + prefix + total;
-            }
-        }
-        __syncthreads();
-        if (s_abort) break;
-        const uint64_t tile_base = base + s_prefix;
-#pragma unroll
-        for (int k = 0; k < kItems; ++k) {
-            if (flags & (1u << k)) {
-                const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-                const uint64_t o = tile_base + s_cnt[k * kWarps + warp] + lane_rank[k];
-                const uint32_t row = rows ? __ldcs(rows + i) : (uint32_t)i;
-                __stcs(reinterpret_cast<unsigned long long*>(pairs + o), ((unsigned long long)pos[k] << 32) | row);
-            }
-        }
-        __syncthreads();
+    };
+    for (;;) {
+        const uint32_t tile = claim_tile(ws);
+        if (tile >= num_tiles) break;
+        if (!pairs_tile<kCompactItems>(load, tile, nullptr, m, pairs, 0ull, d_count, ws, num_tiles)) break;
     }
 }
 
@@ -323,10 +403,16 @@ stage_desc make_stage(const gj_index* idx) {
 size_t stage_bytes(const stage_desc& sd) { return (size_t)(sd.words0 + sd.words1) * sizeof(uint64_t); }
 
 template <class Kernel>
+int prepare_smem(Kernel kernel, size_t smem) {
+    if (smem > 48 * 1024) GJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return GJ_OK;
+}
+
+template <class Kernel>
 int grid_for(Kernel kernel, size_t smem, uint64_t work_items, int* grid) {
     device_info di;
     GJ_TRY(current_device_info(&di));
-    if (smem > 48 * 1024) GJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GJ_TRY(prepare_smem(kernel, smem));
     int per_sm = 0;
     GJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem));
     if (per_sm < 1) per_sm = 1;
@@ -340,9 +426,9 @@ int grid_for(Kernel kernel, size_t smem, uint64_t work_items, int* grid) {
 template <class Op>
 int run_lookup(const Op& op, const stage_desc& sd, const uint64_t* probes, uint64_t m, uint32_t* out, cudaStream_t s) {
     const size_t smem = stage_bytes(sd);
-    int grid = 0;
-    GJ_TRY(grid_for(k_lookup<Op>, smem, (m + kLookupItems - 1) / kLookupItems, &grid));
-    k_lookup<Op><<<grid, kBlock, smem, s>>>(op, sd, probes, m, out);
+    GJ_TRY(prepare_smem(k_lookup<Op>, smem));
+    const uint64_t grid = (m + kLookupTile - 1) / kLookupTile;
+    k_lookup<Op><<<(unsigned)grid, kBlock, smem, s>>>(op, sd, probes, m, out);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
 }
@@ -351,9 +437,9 @@ template <class Op>
 int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const uint32_t* rows, uint64_t m,
                 uint32_t* out, cudaStream_t s) {
     const size_t smem = stage_bytes(sd);
-    int grid = 0;
-    GJ_TRY(grid_for(k_scatter_lookup<Op>, smem, (m + kLookupItems - 1) / kLookupItems, &grid));
-    k_scatter_lookup<Op><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, out);
+    GJ_TRY(prepare_smem(k_scatter_lookup<Op>, smem));
+    const uint64_t grid = (m + kLookupTile - 1) / kLookupTile;
+    k_scatter_lookup<Op><<<(unsigned)grid, kBlock, smem, s>>>(op, sd, keys, rows, m, out);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
 }
@@ -380,6 +466,16 @@ int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const 
         return GJ_OK;
     }
     GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, wc.used, s));
+    if (!rows && !d_base) {
+        GJ_TRY(run_lookup(op, sd, probes, m, pairs + m, s));
+        const uint32_t compact_tiles = (uint32_t)((m + kCompactTile - 1) / kCompactTile);
+        int grid = 0;
+        GJ_TRY(grid_for(k_compact_pairs, 0, (uint64_t)compact_tiles * kBlock, &grid));
+        k_compact_pairs<<<grid, kBlock, 0, s>>>(pairs + m, m, reinterpret_cast<uint2*>(pairs), d_count, pw,
+                                                compact_tiles);
+        GJ_CUDA_TRY(cudaGetLastError());
+        return GJ_OK;
+    }
     const size_t smem = stage_bytes(sd);
     int grid = 0;
     GJ_TRY(grid_for(k_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));

@@ -67,7 +67,7 @@ typedef struct gj_index_params {
     uint32_t struct_size;       /* = sizeof(gj_index_params) */
     uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout + 1): 4, 8, 16, 32 or 64 (default 4:
                                    one 32-byte sector per node) */
-    uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 16) */
+    uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 8) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */
     uint32_t rs_max_error;      /* RadixSpline spline error (default 32) */
     uint32_t bs_cache_keys;     /* binary search: sampled keys staged in shared memory (default 4096, 0 = off) */
@@ -143,6 +143,13 @@ int gj_index_lookup(const gj_index* index, const uint64_t* d_probes, uint64_t m,
 int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Outcome of the last gj_inlj_pairs run on this workspace with this m:
+ * waits on the stream, then returns GJ_OK or
+ * GJ_ERR_TIMEOUT when a bounded device wait of the ordered compaction gave up
+ * (the pairs and *d_count are then incomplete).  No counterpart in the
+ * reference, whose compaction does not wait. */
+int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream);
 
 /* Same pairs as gj_inlj_pairs, for callers that cannot allocate device
  * memory when they probe (a frozen allocator, someone else's memory arena,

@@ -62,6 +62,14 @@ GJ_DEVICE_INLINE uint64_t lower_bound_branch_free(const uint64_t* arr, uint64_t 
     return ret;
 }
 
+// k[i] for a run-time i < 4 without indexing the array (which would put it
+// in local memory)
+GJ_DEVICE_INLINE uint64_t pick4(const uint64_t (&k)[4], uint32_t i) {
+    const uint64_t lo = (i & 1) ? k[1] : k[0];
+    const uint64_t hi = (i & 1) ? k[3] : k[2];
+    return (i & 2) ? hi : lo;
+}
+
 // Lower bound of key in arr[lo, hi) by a binary search over the 32-byte
 // sectors that cover the range.  arr must be 32-byte aligned when aligned is
 // set; arr_n is the number of valid entries of arr (a sector that reaches
@@ -77,26 +85,31 @@ GJ_DEVICE_INLINE uint64_t lower_bound_sectors(const uint64_t* arr, uint64_t arr_
         *eq = r < hi && ld_ro(arr + r) == key;
         return r;
     }
-    uint64_t sl = lo >> 2, sr = (hi - 1) >> 2;
+    // positions are below 2^32 - 1 (columns hold at most 2^32 - 2 keys), so
+    // the search runs on 32-bit positions; hi <= arr_n keeps every sector
+    // start below arr_n
+    const uint32_t lo32 = (uint32_t)lo, hi32 = (uint32_t)hi, n32 = (uint32_t)arr_n;
+    uint32_t sl = lo32 >> 2, sr = (hi32 - 1) >> 2;
     // first in-range position known to hold a key >= key, and that key: the
     // answer may end up there after the sector that holds it was ruled out
-    uint64_t right_pos = hi, right_key = 0;
+    uint32_t right_pos = hi32;
+    uint64_t right_key = 0;
     for (;;) {
-        const uint64_t s = (sl + sr) >> 1;
-        const uint64_t s0 = s << 2;
+        const uint32_t s = (sl + sr) >> 1;
+        const uint32_t s0 = s << 2;
         uint64_t k[4];
-        if (s0 + 4 <= arr_n) {
+        if (n32 - s0 >= 4) {
             ld_sector(arr + s0, k);
         } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) k[i] = (s0 + i < arr_n) ? ld_ro(arr + s0 + i) : ~0ull;
+            for (uint32_t i = 0; i < 4; ++i) k[i] = (i < n32 - s0) ? ld_ro(arr + s0 + i) : ~0ull;
         }
-        const uint64_t first = s0 > lo ? s0 : lo;
-        const uint64_t last = s0 + 4 < hi ? s0 + 4 : hi;
+        const uint32_t first = s0 > lo32 ? s0 : lo32;
+        const uint32_t last = hi32 - s0 > 4 ? s0 + 4 : hi32;
         uint32_t below = 0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) below += (s0 + i >= first && s0 + i < last && k[i] < key) ? 1u : 0u;
-        const uint32_t in_range = (uint32_t)(last - first);
+        for (uint32_t i = 0; i < 4; ++i) below += (s0 + i >= first && s0 + i < last && k[i] < key) ? 1u : 0u;
+        const uint32_t in_range = last - first;
         if (below == in_range) {  // every in-range key of the sector is < key
             if (s == sr) {
                 *eq = last == right_pos && right_key == key;
@@ -105,11 +118,11 @@ GJ_DEVICE_INLINE uint64_t lower_bound_sectors(const uint64_t* arr, uint64_t arr_
             sl = s + 1;
         } else if (below == 0 && s != sl) {  // every in-range key is >= key, earlier sectors remain
             right_pos = first;
-            right_key = k[first - s0];
+            right_key = pick4(k, first - s0);
             sr = s - 1;
         } else {
-            const uint64_t r = first + below;
-            *eq = k[r - s0] == key;
+            const uint32_t r = first + below;
+            *eq = pick4(k, r - s0) == key;
             return r;
         }
     }
@@ -209,17 +222,16 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
 template <int W>
 GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
     if (key > v.max_key) return kInvalid;
-    constexpr uint64_t F = W + 1;
-    uint64_t j = 0;
+    constexpr uint32_t F = W + 1;
+    // node and leaf numbers are below 2^32 (at most one leaf per key)
+    uint32_t j = 0;
     const int h = (int)v.height;
     const int first_global = h - (int)v.cached_levels;  // levels <= this come from global memory
-    for (int l = h; l >= 1; --l) {
-        const bool sm = l > first_global;
-        const uint64_t* node = sm ? cache + v.smem_offset[l] + j * W : v.level[l] + j * W;
-        j = j * F + btree_node_search<W>(node, key, sm);
-    }
+    int l = h;
+    for (; l > first_global; --l) j = j * F + btree_node_search<W>(cache + v.smem_offset[l] + j * W, key, true);
+    for (; l >= 1; --l) j = j * F + btree_node_search<W>(v.level[l] + (uint64_t)j * W, key, false);
     // leaf j: column slice [j*L, min(j*L + L, n))
-    const uint64_t base = j * v.leaf_keys;
+    const uint64_t base = (uint64_t)j * v.leaf_keys;
     const uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
     bool eq;
     const uint64_t pos = lower_bound_sectors(v.col, v.n, base, end, key, v.col_aligned, &eq);

@@ -30,6 +30,36 @@ def test_inlj_pairs_match_oracle(orc, gj, cuda, kind, m):
     np.testing.assert_array_equal(pos, epos)
 
 
+@pytest.mark.parametrize("kind", ["btree", "learned", "no_op"])
+@pytest.mark.parametrize("m", [4095, 4096, 4097, 3 * 1000 * 1000 + 17])
+def test_inlj_pairs_compaction_tiles(orc, gj, cuda, kind, m):
+    # plain pairs are positions first (parked in the upper half of the pairs
+    # buffer), then an ordered compaction over 4096-probe tiles with a
+    # look-back over many predecessors; the workspace is reused across calls
+    import torch
+
+    rng = np.random.default_rng(m)
+    col = column(rng, 32 * 4000)
+    pr = probes_for(rng, col, m)[:m]
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    d_pr = to_dev(torch, pr)
+    ws = None
+    for _ in range(2):
+        out, cnt = ix.inlj_pairs(d_pr, workspace=ws)
+        if ws is None:
+            import ctypes
+
+            need = ctypes.c_size_t(0)
+            gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(need))
+            ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+            out, cnt = ix.inlj_pairs(d_pr, workspace=ws)
+        ix.inlj_pairs_status(ws, m)
+        rows, pos = pairs_of(out, cnt)
+        erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
+        np.testing.assert_array_equal(rows, erows)
+        np.testing.assert_array_equal(pos, epos)
+
+
 def test_inlj_pairs_all_absent(orc, gj, cuda):
     import torch
 
