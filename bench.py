@@ -541,6 +541,17 @@ def learned_workload(args, world, rank, device, stream):
                 entry.update({"max_error": me, "mean_window": round(mw, 2)})
             row[kind] = entry
             ix.free()
+        # RadixSpline at the learned model's recorded error bound (equal epsilon)
+        eps = int(min(row["learned_mlp"]["max_error"], (1 << 31) - 1))
+        ix = gj.radix_spline_index(rs_max_error=max(eps, 1)).construct(None, keys)
+        ms = time_steps(lambda: ix.lookup(probes, out), args.steps, args.warmup, stream, world, device)
+        row["radix_spline_same_eps"] = {"tuples_per_s": m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                                        "exact": bool(torch.equal(out, ref)), "max_error": eps,
+                                        "index_bytes": ix.memory_consumption()}
+        ix.free()
+        best_learned = max(row["learned_mlp"]["tuples_per_s"], row["learned_linear"]["tuples_per_s"])
+        row["learned_beats"] = {k: best_learned > row[k]["tuples_per_s"]
+                                for k in ("binary_search", "radix_spline", "radix_spline_same_eps")}
         results[dist_name] = row
         del keys, probes
     head = results["uniform"]["learned_mlp"]
@@ -598,7 +609,7 @@ def batch_workload(args, world, rank, device, stream):
             bs = sizes[r]
             offs = np.concatenate([[0], np.cumsum(bs)[:-1]]).astype(np.uint64)
             for j, b in enumerate(r):
-                probes[offs[j]: offs[j] + bs[j]] = gj.generate_probes(cols[which[b]], int(bs[j]), theta=0.8,
+                probes[int(offs[j]): int(offs[j] + bs[j])] = gj.generate_probes(cols[which[b]], int(bs[j]), theta=0.8,
                                                                        seed=args.seed + int(b))
             start_ev = torch.cuda.Event(enable_timing=True)
             end_ev = torch.cuda.Event(enable_timing=True)

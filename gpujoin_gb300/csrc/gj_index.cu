@@ -317,12 +317,12 @@ void gj_index_params_default(gj_index_params* p) {
     p->rs_max_error = 32;
     p->bs_cache_keys = 4096;
     p->smem_cache_bytes = 16384;
-    p->learned_leaves = 16384;
+    p->learned_leaves = 65536;
     p->learned_root = GJ_LEARNED_ROOT_MLP;
     p->learned_hidden = 32;
     p->learned_steps = 600;
     p->learned_batch = 8192;
-    p->learned_lr = 3e-3f;
+    p->learned_lr = 1e-3f;
     p->seed = 0x5eedULL;
 }
 
@@ -517,8 +517,9 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
         set_error("gj_inlj_pairs: probe rows must fit 32 bits");
         return GJ_ERR_TOO_LARGE;
     }
+    // positions are parked in the upper half of the pairs buffer (2m u32)
     return launch_pairs(index, d_probes, m, nullptr, d_pairs, nullptr, d_count, d_workspace, workspace_bytes,
-                        as_stream(stream));
+                        d_pairs ? d_pairs + m : nullptr, as_stream(stream));
 }
 
 int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream) {

@@ -112,8 +112,11 @@ struct gj_index {
     gj::harmonia_view hm{};
     gj::rs_view rs{};
     gj::learned_view ln{};
+    gj::learned_root_params ln_root{};  // host copy of the root parameters (kernel arguments)
     uint64_t learned_max_error = 0;
     double learned_mean_window = 0.0;
+    double learned_init_loss = 0.0;     // root MLP: sample loss of the quantile start
+    double learned_trained_loss = 0.0;  // root MLP: sample loss after training
 
     size_t smem_bytes = 0;          // dynamic shared memory of the lookup kernels
     const uint64_t* smem_src = nullptr;  // device source of the staged cache
@@ -125,10 +128,21 @@ namespace gj {
 int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s);
 int launch_scatter_lookup(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
                           uint32_t* d_out, cudaStream_t s);
-// pairs are written from offset *d_base (0 if null); *d_count = base + matches
+// Pairs are written from offset *d_base (0 if null); *d_count = base +
+// matches.  With d_stash the probes take two passes (search, then ordered
+// compaction) and their positions are parked in d_stash: m u32 inside the
+// pairs buffer at or after u32 index 2 * (largest possible base) + m, so
+// that pair o only overlaps stash entries j <= o.  Without it, one pass.
 int launch_pairs(const gj_index* idx, const uint64_t* d_probes, uint64_t m, const uint32_t* d_rows,
                  uint32_t* d_pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
-                 cudaStream_t s);
+                 uint32_t* d_stash, cudaStream_t s);
+// Pairs of a partitioned relation (keys grouped by key range, row ids
+// attached): every tile of probes is sorted by key before it is searched.
+// Pairs are appended at *d_base; the order inside a tile is not fixed.
+// Workspace: pairs_workspace_bytes(m).
+int launch_partitioned_pairs(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
+                             uint32_t* d_pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
+                             cudaStream_t s);
 size_t pairs_workspace_bytes(uint64_t m);
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s);
 

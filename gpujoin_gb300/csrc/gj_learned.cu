@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "gj_internal.h"
@@ -221,7 +222,7 @@ __global__ void k_route(learned_view v, const float* __restrict__ root, uint32_t
                         unsigned int* __restrict__ first, unsigned int* __restrict__ last,
                         unsigned int* __restrict__ count) {
     extern __shared__ float s_root[];
-    const int np = v.root_kind == GJ_LEARNED_ROOT_MLP ? (int)mlp_param_count(v.hidden) : 2;
+    const int np = v.root_kind == GJ_LEARNED_ROOT_MLP ? kMlpParams : 2;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s_root[i] = root[i];
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -312,25 +313,31 @@ struct scratch {
     }
 };
 
-void init_mlp(std::vector<float>& P, uint32_t H, uint64_t seed) {
+// Quantile initialisation: the network starts as the piecewise-linear CDF
+// through H + 1 sample quantiles (q_j, y_j): h1_j = relu(x - q_j), layer 2
+// passes h1 through (identity weights; h1 >= 0), and the output weights are
+// the slope changes at the knots.  Training then refines this fit.
+void init_mlp_quantiles(std::vector<float>& P, uint32_t H, const std::vector<float>& q, const std::vector<float>& y) {
     const uint32_t np = mlp_param_count(H);
     P.assign(np, 0.f);
-    auto uni = [&](uint64_t i, float a) {
-        const double u = (double)(mix64(mix64(seed ^ 0x1117ull) + i) >> 11) * (1.0 / 9007199254740992.0);
-        return (float)((2.0 * u - 1.0) * a);
-    };
-    // first layer: ReLU kinks spread over [0, 1] (b1 = -t * w with t in [0, 1))
+    float* W1 = P.data();
+    float* b1 = W1 + H;
+    float* W2 = b1 + H;
+    float* b2 = W2 + H * H;
+    float* W3 = b2 + H;
+    float* b3 = W3 + H;
+    double prev = 0.0;
     for (uint32_t j = 0; j < H; ++j) {
-        const float w = 1.0f + std::fabs(uni(j, 1.0f));
-        const float t = (float)j / (float)H;
-        P[j] = w;
-        P[H + j] = -t * w;
+        W1[j] = 1.f;
+        b1[j] = -q[j];
+        W2[j * H + j] = 1.f;
+        b2[j] = 0.f;
+        const double dq = std::max(1e-7, (double)q[j + 1] - (double)q[j]);
+        const double slope = ((double)y[j + 1] - (double)y[j]) / dq;
+        W3[j] = (float)(slope - prev);
+        prev = slope;
     }
-    const float a2 = std::sqrt(6.0f / (float)H);
-    for (uint32_t i = 0; i < H * H; ++i) P[2 * H + i] = uni(1000 + i, a2) * 0.5f;
-    for (uint32_t o = 0; o < H; ++o) P[2 * H + H * H + o] = 0.01f;
-    for (uint32_t o = 0; o < H; ++o) P[3 * H + H * H + o] = uni(5000 + o, 1.0f / std::sqrt((float)H));
-    P[4 * H + H * H] = 0.f;
+    b3[0] = y[0];
 }
 
 }  // namespace
@@ -391,18 +398,18 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     v.hidden = H;
     v.col_aligned = column_aligned32(idx->d_col);
 
-    const uint32_t np = p.learned_root == GJ_LEARNED_ROOT_MLP ? mlp_param_count(H) : 2;
-    const uint32_t np_padded = (np + 1) & ~1u;  // staged as 64-bit words
+    const uint32_t np = p.learned_root == GJ_LEARNED_ROOT_MLP ? mlp_param_count(H) : 2;  // trained parameters
+    const uint32_t nstored = p.learned_root == GJ_LEARNED_ROOT_MLP ? (uint32_t)kMlpParams : 2u;
     void* root_mem = nullptr;
     void* leaf_mem = nullptr;
-    GJ_TRY(device_alloc_for(idx, np_padded * sizeof(float), &root_mem));
+    GJ_TRY(device_alloc_for(idx, nstored * sizeof(float), &root_mem));
     GJ_TRY(device_alloc_for(idx, (size_t)L * sizeof(learned_leaf), &leaf_mem));
     float* d_root = static_cast<float*>(root_mem);
     v.root = d_root;
     v.leaves = static_cast<learned_leaf*>(leaf_mem);
-    GJ_CUDA_TRY(cudaMemsetAsync(d_root, 0, np_padded * sizeof(float), s));
-    idx->smem_words = np_padded / 2;
-    idx->bytes = np_padded * sizeof(float) + (uint64_t)L * sizeof(learned_leaf);
+    idx->smem_words = 0;  // the lookup kernels take the root parameters by value
+    idx->bytes = nstored * sizeof(float) + (uint64_t)L * sizeof(learned_leaf);
+    std::memset(&idx->ln_root, 0, sizeof(idx->ln_root));
 
     scratch sc;
     // training samples
@@ -432,13 +439,27 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         const double den = N * sxx - sx * sx;
         const double a = den != 0.0 ? (N * sxy - sx * sy) / den : 0.0;
         const double b = (sy - a * sx) / N;
-        const float ab[2] = {(float)a, (float)b};
-        GJ_CUDA_TRY(cudaMemcpyAsync(d_root, ab, sizeof(ab), cudaMemcpyHostToDevice, s));
-        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+        idx->ln_root.w[0] = (float)a;
+        idx->ln_root.w[1] = (float)b;
     } else {
+        // start from the piecewise-linear CDF through H + 1 sample quantiles
+        std::vector<float> hx(S), hy(S);
+        GJ_CUDA_TRY(cudaMemcpyAsync(hx.data(), xs, S * sizeof(float), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(hy.data(), ys, S * sizeof(float), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+        std::vector<float> q(H + 1), qy(H + 1);
+        for (uint32_t j = 0; j < H; ++j) {
+            const uint64_t at = (uint64_t)j * S / H;
+            q[j] = hx[at];
+            qy[j] = hy[at];
+        }
+        q[H] = 1.f;
+        qy[H] = 1.f;
         std::vector<float> P0;
-        init_mlp(P0, H, p.seed);
-        GJ_CUDA_TRY(cudaMemcpyAsync(d_root, P0.data(), np * sizeof(float), cudaMemcpyHostToDevice, s));
+        init_mlp_quantiles(P0, H, q, qy);
+        float* d_train = nullptr;  // trained parameters (H wide)
+        GJ_TRY(sc.alloc(np, &d_train));
+        GJ_CUDA_TRY(cudaMemcpyAsync(d_train, P0.data(), np * sizeof(float), cudaMemcpyHostToDevice, s));
         const uint32_t B = std::max<uint32_t>(kTrainBlock, std::min<uint32_t>(p.learned_batch, 1u << 16));
         const int nblocks = (int)((B + kTrainBlock - 1) / kTrainBlock);
         float *partial = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
@@ -461,14 +482,40 @@ int build_learned(gj_index* idx, cudaStream_t s) {
             // cosine-decayed learning rate
             const float lr = p.learned_lr * 0.5f * (1.f + std::cos(3.14159265f * (float)t / (float)T));
             k_batch_indices<<<(B + 255) / 256, 256, 0, s>>>(bidx, B, S, p.seed ^ 0xb47c4ull, t);
-            k_mlp_grad<<<nblocks, kTrainBlock, smem, s>>>(d_root, (int)H, xs, ys, B, bidx, 1.0f / (float)B, partial,
+            k_mlp_grad<<<nblocks, kTrainBlock, smem, s>>>(d_train, (int)H, xs, ys, B, bidx, 1.0f / (float)B, partial,
                                                           nullptr);
             k_reduce_partials<<<(np + 255) / 256, 256, 0, s>>>(partial, (int)np, nblocks, grad, nullptr, nullptr);
-            k_adam<<<(np + 255) / 256, 256, 0, s>>>(d_root, grad, m1, m2, (int)np, lr, b1, b2, 1e-8f, 1.f - c1,
+            k_adam<<<(np + 255) / 256, 256, 0, s>>>(d_train, grad, m1, m2, (int)np, lr, b1, b2, 1e-8f, 1.f - c1,
                                                     1.f - c2);
         }
         GJ_CUDA_TRY(cudaGetLastError());
+        // keep the trained network unless it fits the samples worse than its start
+        std::vector<float> P1(np);
+        GJ_CUDA_TRY(cudaMemcpyAsync(P1.data(), d_train, np * sizeof(float), cudaMemcpyDeviceToHost, s));
+        double* d_loss = nullptr;
+        GJ_TRY(sc.alloc(2, &d_loss));
+        GJ_TRY(mlp_grad(d_train, H, xs, ys, S, grad, d_loss, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(d_train, P0.data(), np * sizeof(float), cudaMemcpyHostToDevice, s));
+        GJ_TRY(mlp_grad(d_train, H, xs, ys, S, grad, d_loss + 1, s));
+        double losses[2] = {0, 0};
+        GJ_CUDA_TRY(cudaMemcpyAsync(losses, d_loss, sizeof(losses), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+        const std::vector<float>& best = losses[0] <= losses[1] ? P1 : P0;
+        idx->learned_trained_loss = losses[0];
+        idx->learned_init_loss = losses[1];
+        // store zero-padded to the 32-wide layout of the lookup
+        constexpr uint32_t W = kMlpWidth;
+        float* out = idx->ln_root.w;
+        for (uint32_t j = 0; j < H; ++j) {
+            out[j] = best[j];              // W1
+            out[W + j] = best[H + j];      // b1
+            for (uint32_t i = 0; i < H; ++i) out[2 * W + j * W + i] = best[2 * H + j * H + i];  // W2 row j
+            out[2 * W + W * W + j] = best[2 * H + H * H + j];                                  // b2
+            out[3 * W + W * W + j] = best[3 * H + H * H + j];                                  // W3
+        }
+        out[4 * W + W * W] = best[4 * H + H * H];  // b3
     }
+    GJ_CUDA_TRY(cudaMemcpyAsync(d_root, idx->ln_root.w, nstored * sizeof(float), cudaMemcpyHostToDevice, s));
 
     // route every key, fit the leaves, measure their error windows
     uint32_t* leaf_of = nullptr;
@@ -480,7 +527,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     GJ_CUDA_TRY(cudaMemsetAsync(first, 0xFF, L * sizeof(unsigned int), s));
     GJ_CUDA_TRY(cudaMemsetAsync(last, 0, L * sizeof(unsigned int), s));
     GJ_CUDA_TRY(cudaMemsetAsync(count, 0, L * sizeof(unsigned int), s));
-    k_route<<<grid_for_n(n), 256, np_padded * sizeof(float), s>>>(v, d_root, leaf_of, first, last, count);
+    k_route<<<grid_for_n(n), 256, nstored * sizeof(float), s>>>(v, v.root, leaf_of, first, last, count);
     k_leaf_params<<<(L + 255) / 256, 256, 0, s>>>(idx->d_col, L, first, last, count,
                                                  const_cast<learned_leaf*>(v.leaves));
     k_leaf_error<<<grid_for_n(n), 256, 0, s>>>(v, leaf_of, const_cast<learned_leaf*>(v.leaves));

@@ -13,6 +13,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "gj_internal.h"
 
@@ -73,11 +76,14 @@ struct op_noop {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
 };
+// the root parameters travel inside the op (a kernel argument): the MLP's
+// FMAs read their weights from the constant bank
 struct op_learned {
     static constexpr int kMinBlocks = GJ_BLOCKS(4);
     learned_view v;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
-        return learned_lookup(v, reinterpret_cast<const float*>(cache), key);
+    learned_root_params p;
+    __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const {
+        return learned_lookup(v, p.w, key);
     }
 };
 
@@ -110,10 +116,10 @@ __device__ __forceinline__ uint64_t load_probe(const uint64_t* p, uint64_t i, ui
 }
 
 template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_lookup(const __grid_constant__ Op op, const stage_desc sd,
                                                    const uint64_t* __restrict__ probes, uint64_t m,
                                                    uint32_t* __restrict__ out) {
-    extern __shared__ uint64_t cache[];
+    extern __shared__ __align__(16) uint64_t cache[];
     stage_cache(cache, sd);
     const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
     uint64_t next = load_probe(probes, t0, m);
@@ -129,11 +135,11 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_lookup(const Op op, 
 
 // scattered lookup over a partitioned relation: out[rows[i]] = lookup(keys[i])
 template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const Op op, const stage_desc sd,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const __grid_constant__ Op op, const stage_desc sd,
                                                            const uint64_t* __restrict__ keys,
                                                            const uint32_t* __restrict__ rows, uint64_t m,
                                                            uint32_t* __restrict__ out) {
-    extern __shared__ uint64_t cache[];
+    extern __shared__ __align__(16) uint64_t cache[];
     stage_cache(cache, sd);
     const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
     uint64_t next = load_probe(keys, t0, m);
@@ -165,7 +171,10 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const
 constexpr int kItems = GJ_LOOKUP_ITEMS;          // k_pairs items per thread
 constexpr int kCompactItems = 16;                // k_compact_pairs items per thread
 static_assert(kItems >= 4 && (kItems & (kItems - 1)) == 0, "the pairs scan needs a power-of-two item count >= 4");
-constexpr uint32_t kTile = kBlock * kItems;      // also the workspace's tile unit (the larger tile count)
+constexpr uint32_t kTile = kBlock * kItems;
+// the workspace holds one state per kStateTile probes: enough for the
+// smallest tile of any pairs kernel, at the same offsets for all of them
+constexpr uint32_t kStateTile = kBlock * 4;
 constexpr uint32_t kCompactTile = kBlock * kCompactItems;
 constexpr unsigned long long kFlagAggregate = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
@@ -177,6 +186,17 @@ struct pairs_ws {
     unsigned int* tile_counter;      // 1
     unsigned int* error;             // 1
 };
+
+// the workspace layout of every pairs kernel; false when it is too small
+inline bool carve_pairs_ws(void* ws, size_t ws_bytes, uint64_t m, pairs_ws* pw, size_t* used) {
+    const uint64_t states = (m + kStateTile - 1) / kStateTile;
+    workspace_carver wc(ws, ws_bytes);
+    pw->tile_state = wc.take<unsigned long long>(states ? states : 1);
+    pw->tile_counter = wc.take<unsigned int>(2);
+    pw->error = pw->tile_counter ? pw->tile_counter + 1 : nullptr;
+    *used = wc.used;
+    return pw->tile_state && pw->tile_counter;
+}
 
 // Exclusive prefix of tile `tile` (> 0) from the states of its predecessors,
 // read 32 at a time by the calling warp: lane i reads tile j - i, and the
@@ -212,14 +232,14 @@ __device__ __forceinline__ bool look_back(const pairs_ws& ws, uint32_t tile, uin
 }
 
 // One block-tile of the ordered compaction: fill(t0, s_pos) writes the
-// result of probe t0 + j into s_pos[j] (kInvalid for no pair) for the
-// tile's kBlock * kIt probes; the block then emits the pairs of the tile at
-// the tile's prefix.  Returns false when the kernel must stop (look-back
-// timed out).
-template <int kIt, class Fill>
-__device__ __forceinline__ bool pairs_tile(Fill&& fill, uint32_t tile, const uint32_t* __restrict__ rows, uint64_t m,
-                                           uint2* pairs, uint64_t base, uint64_t* __restrict__ d_count,
-                                           const pairs_ws& ws, uint32_t num_tiles) {
+// result of tile item j into s_pos[j] (kInvalid for no pair) for the tile's
+// kBlock * kIt items; the block then emits the pairs of the tile, in item
+// order, at the tile's prefix.  row_of(k, i) is the probe row of item k of
+// the calling thread (i = t0 + k * kBlock + thread).  Returns false when the
+// kernel must stop (look-back timed out).
+template <int kIt, class Fill, class RowOf>
+__device__ __forceinline__ bool pairs_tile(Fill&& fill, RowOf&& row_of, uint32_t tile, uint2* pairs, uint64_t base,
+                                           uint64_t* __restrict__ d_count, const pairs_ws& ws, uint32_t num_tiles) {
     constexpr int kWarps = kBlock / 32;
     constexpr uint32_t kT = kBlock * kIt;
     __shared__ uint32_t s_cnt[kIt * kWarps];
@@ -297,7 +317,7 @@ __device__ __forceinline__ bool pairs_tile(Fill&& fill, uint32_t tile, const uin
             const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
             const uint32_t rank = __popc(s_ballot[k * kWarps + warp] & ((1u << lane) - 1u));
             const uint64_t o = tile_base + s_cnt[k * kWarps + warp] + rank;
-            const uint32_t row = rows ? __ldcs(rows + i) : (uint32_t)i;
+            const uint32_t row = row_of(k, i);
             const uint32_t pos = s_pos[k * kBlock + threadIdx.x];
             __stcs(reinterpret_cast<unsigned long long*>(pairs + o), ((unsigned long long)pos << 32) | row);
         }
@@ -316,11 +336,11 @@ __device__ __forceinline__ uint32_t claim_tile(const pairs_ws& ws) {
 // single pass: search and compact tile by tile (partitioned relations, whose
 // pairs are appended behind *d_base)
 template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const __grid_constant__ Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
                                                   const uint32_t* __restrict__ rows, uint64_t m,
                                                   uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
                                                   uint64_t* __restrict__ d_count, pairs_ws ws, uint32_t num_tiles) {
-    extern __shared__ uint64_t cache[];
+    extern __shared__ __align__(16) uint64_t cache[];
     stage_cache(cache, sd);
     const uint64_t base = d_base ? *d_base : 0ull;
     auto search = [&](uint64_t t0, uint32_t* s_pos) {
@@ -336,20 +356,24 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const Op op, c
     for (;;) {
         const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
-        if (!pairs_tile<kItems>(search, tile, rows, m, pairs, base, d_count, ws, num_tiles)) break;
+        auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
+        if (!pairs_tile<kItems>(search, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
     }
 }
 
 // Second pass of the two-pass pairs: compact the positions k_lookup wrote
-// to the upper half of the pairs buffer (u32 index m + i) into pairs.  A
-// tile writes pairs only after every earlier tile has published its count,
-// i.e. after every earlier tile has read its positions, and pair o covers
-// u32 indices 2o and 2o+1 < m + i for the tile's own probes i >= o: no
-// position is overwritten before it is read.  (stash and pairs alias, so
-// neither is __restrict__.)
-__global__ void __launch_bounds__(kBlock) k_compact_pairs(const uint32_t* stash, uint64_t m, uint2* pairs,
+// to the stash into pairs at *d_base + (rank of the match).  The stash lies
+// inside the pairs buffer, placed so that the u32 words of pair o only reach
+// stash entries j <= o: a tile writes pairs only after every earlier tile
+// has published its count, i.e. after every earlier tile has read its
+// positions, so no position is overwritten before it is read.  (stash and
+// pairs alias, so neither is __restrict__.)
+__global__ void __launch_bounds__(kBlock) k_compact_pairs(const uint32_t* stash, const uint32_t* __restrict__ rows,
+                                                          uint64_t m, uint2* pairs,
+                                                          const uint64_t* __restrict__ d_base,
                                                           uint64_t* __restrict__ d_count, pairs_ws ws,
                                                           uint32_t num_tiles) {
+    const uint64_t base = d_base ? *d_base : 0ull;
     auto load = [&](uint64_t t0, uint32_t* s_pos) {
 #pragma unroll
         for (int k = 0; k < kCompactItems; ++k) {
@@ -360,7 +384,137 @@ __global__ void __launch_bounds__(kBlock) k_compact_pairs(const uint32_t* stash,
     for (;;) {
         const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
-        if (!pairs_tile<kCompactItems>(load, tile, nullptr, m, pairs, 0ull, d_count, ws, num_tiles)) break;
+        auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
+        if (!pairs_tile<kCompactItems>(load, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
+    }
+}
+
+// Pairs of a partitioned relation (probes grouped by key range, rows
+// attached).  Each tile of kTile probes is first sorted by key in shared
+// memory -- a counting sort over kSortBuckets equal-width buckets of the
+// tile's key range -- and then searched in that order: neighbouring lanes
+// follow the same path through the upper index levels, and a warp-wide load
+// of one sector serves all lanes that ask for it.  Pairs leave in tile order
+// (sorted within a tile, in the relation's order across tiles); the order of
+// equal-bucket keys inside a tile is not fixed.
+constexpr int kSortItems = 4;                        // probes per thread and tile
+constexpr uint32_t kSortTile = kBlock * kSortItems;  // 1024
+constexpr uint32_t kSortBuckets = kSortTile;
+static_assert(kStateTile <= kSortTile && kStateTile <= kTile && kStateTile <= kCompactTile,
+              "the workspace needs a state per tile of every pairs kernel");
+
+__device__ __forceinline__ unsigned bit_length(uint64_t v) { return v ? 64u - (unsigned)__clzll(v) : 0u; }
+
+// about 21 KB of shared memory per block; 6 resident blocks (40 registers),
+// fewer for index kinds compiled for fewer
+template <class Op>
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 6) k_sorted_pairs(const __grid_constant__ Op op, const stage_desc sd,
+                                                         const uint64_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ rows, uint64_t m,
+                                                         uint2* __restrict__ pairs,
+                                                         const uint64_t* __restrict__ d_base,
+                                                         uint64_t* __restrict__ d_count, pairs_ws ws,
+                                                         uint32_t num_tiles) {
+    extern __shared__ __align__(16) uint64_t cache[];
+    constexpr int kWarps = kBlock / 32;
+    __shared__ uint64_t s_key[kSortTile];
+    __shared__ uint32_t s_row[kSortTile];
+    __shared__ __align__(16) uint32_t s_bucket[kSortBuckets];  // read as uint4
+    __shared__ unsigned long long s_lo[kWarps], s_hi[kWarps];
+    stage_cache(cache, sd);
+    const uint64_t base = d_base ? *d_base : 0ull;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto fill = [&](uint64_t t0, uint32_t* s_pos) {
+        const uint32_t tn = m - t0 < kSortTile ? (uint32_t)(m - t0) : kSortTile;
+        uint64_t key[kSortItems];
+        unsigned long long lo = ~0ull, hi = 0ull;
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            key[k] = j < tn ? __ldcs(reinterpret_cast<const unsigned long long*>(keys) + t0 + j) : 0ull;
+            if (j < tn) {
+                lo = key[k] < lo ? key[k] : lo;
+                hi = key[k] > hi ? key[k] : hi;
+            }
+        }
+        // key range of the tile
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) {
+            const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, d);
+            const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, d);
+            lo = a < lo ? a : lo;
+            hi = b > hi ? b : hi;
+        }
+        if (lane == 0) {
+            s_lo[warp] = lo;
+            s_hi[warp] = hi;
+        }
+        for (uint32_t b = threadIdx.x; b < kSortBuckets; b += kBlock) s_bucket[b] = 0;
+        __syncthreads();
+        lo = s_lo[0];
+        hi = s_hi[0];
+#pragma unroll
+        for (int w = 1; w < kWarps; ++w) {
+            lo = s_lo[w] < lo ? s_lo[w] : lo;
+            hi = s_hi[w] > hi ? s_hi[w] : hi;
+        }
+        const unsigned used = bit_length(hi - lo);
+        constexpr unsigned kBucketBits = 10;  // kSortBuckets = 2^10
+        const unsigned sh = used > kBucketBits ? used - kBucketBits : 0;  // (hi - lo) >> sh < kSortBuckets
+        // counting sort: ranks inside a bucket from shared-memory atomics
+        uint32_t rank[kSortItems];
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            rank[k] = j < tn ? atomicAdd(&s_bucket[(uint32_t)((key[k] - lo) >> sh)], 1u) : 0u;
+        }
+        __syncthreads();
+        {
+            // exclusive scan of the buckets: kSortBuckets / kBlock consecutive per thread
+            static_assert(kSortBuckets / kBlock == 4, "one uint4 per thread");
+            uint4* sb = reinterpret_cast<uint4*>(s_bucket) + threadIdx.x;
+            const uint4 c0 = sb[0];
+            const uint32_t sum = c0.x + c0.y + c0.z + c0.w;
+            uint32_t incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (uint32_t)d) incl += t;
+            }
+            __shared__ uint32_t s_wsum[kWarps];
+            if (lane == 31) s_wsum[warp] = incl;
+            __syncthreads();
+            uint32_t run = incl - sum;
+            for (int w = 0; w < (int)warp; ++w) run += s_wsum[w];
+            uint4 o0;
+            o0.x = run; run += c0.x;
+            o0.y = run; run += c0.y;
+            o0.z = run; run += c0.z;
+            o0.w = run;
+            sb[0] = o0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            if (j < tn) {
+                const uint32_t q = s_bucket[(uint32_t)((key[k] - lo) >> sh)] + rank[k];
+                s_key[q] = key[k];
+                s_row[q] = __ldcs(rows + t0 + j);
+            }
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            s_pos[j] = j < tn ? op(cache, s_key[j]) : kInvalid;
+        }
+    };
+    auto row_of = [&](int k, uint64_t) { return s_row[k * kBlock + threadIdx.x]; };
+    for (;;) {
+        const uint32_t tile = claim_tile(ws);
+        if (tile >= num_tiles) break;
+        if (!pairs_tile<kSortItems>(fill, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
     }
 }
 
@@ -390,10 +544,6 @@ stage_desc make_stage(const gj_index* idx) {
                 sd.words1 = idx->hm.cached_nodes;
             }
             break;
-        case GJ_INDEX_LEARNED:
-            sd.src0 = reinterpret_cast<const uint64_t*>(idx->ln.root);
-            sd.words0 = idx->smem_words;
-            break;
         default:
             break;
     }
@@ -404,7 +554,20 @@ size_t stage_bytes(const stage_desc& sd) { return (size_t)(sd.words0 + sd.words1
 
 template <class Kernel>
 int prepare_smem(Kernel kernel, size_t smem) {
-    if (smem > 48 * 1024) GJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // Static plus dynamic shared memory above 48 KB needs the kernel's
+    // dynamic limit raised first; the limit set so far is remembered per
+    // (device, kernel), so the attribute call is made once per new maximum.
+    if (smem == 0) return GJ_OK;
+    int dev = 0;
+    GJ_CUDA_TRY(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> raised;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = raised[{dev, reinterpret_cast<const void*>(kernel)}];
+    if (smem > cur) {
+        GJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cur = smem;
+    }
     return GJ_OK;
 }
 
@@ -446,14 +609,12 @@ int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const 
 
 template <class Op>
 int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const uint32_t* rows, uint64_t m,
-              uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, cudaStream_t s) {
+              uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* stash,
+              cudaStream_t s) {
     const uint32_t num_tiles = (uint32_t)((m + kTile - 1) / kTile);
-    workspace_carver wc(ws, ws_bytes);
     pairs_ws pw;
-    pw.tile_state = wc.take<unsigned long long>(num_tiles ? num_tiles : 1);
-    pw.tile_counter = wc.take<unsigned int>(2);
-    pw.error = pw.tile_counter + 1;
-    if (!pw.tile_state || !pw.tile_counter) {
+    size_t used = 0;
+    if (!carve_pairs_ws(ws, ws_bytes, m, &pw, &used)) {
         set_error("inlj pairs: workspace of %zu bytes is smaller than the %zu required", ws_bytes,
                   pairs_workspace_bytes(m));
         return GJ_ERR_WORKSPACE;
@@ -465,13 +626,13 @@ int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const 
             GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
         return GJ_OK;
     }
-    GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, wc.used, s));
-    if (!rows && !d_base) {
-        GJ_TRY(run_lookup(op, sd, probes, m, pairs + m, s));
+    GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
+    if (stash) {
+        GJ_TRY(run_lookup(op, sd, probes, m, stash, s));
         const uint32_t compact_tiles = (uint32_t)((m + kCompactTile - 1) / kCompactTile);
         int grid = 0;
         GJ_TRY(grid_for(k_compact_pairs, 0, (uint64_t)compact_tiles * kBlock, &grid));
-        k_compact_pairs<<<grid, kBlock, 0, s>>>(pairs + m, m, reinterpret_cast<uint2*>(pairs), d_count, pw,
+        k_compact_pairs<<<grid, kBlock, 0, s>>>(stash, rows, m, reinterpret_cast<uint2*>(pairs), d_base, d_count, pw,
                                                 compact_tiles);
         GJ_CUDA_TRY(cudaGetLastError());
         return GJ_OK;
@@ -485,6 +646,35 @@ int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const 
     return GJ_OK;
 }
 
+template <class Op>
+int run_sorted_pairs(const Op& op, const stage_desc& sd, const uint64_t* keys, const uint32_t* rows, uint64_t m,
+                     uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
+                     cudaStream_t s) {
+    const uint32_t num_tiles = (uint32_t)((m + kSortTile - 1) / kSortTile);
+    pairs_ws pw;
+    size_t used = 0;
+    if (!carve_pairs_ws(ws, ws_bytes, m, &pw, &used)) {
+        set_error("partitioned pairs: workspace of %zu bytes is smaller than the %zu required", ws_bytes,
+                  pairs_workspace_bytes(m));
+        return GJ_ERR_WORKSPACE;
+    }
+    if (m == 0) {
+        if (d_base && d_base != d_count)
+            GJ_CUDA_TRY(cudaMemcpyAsync(d_count, d_base, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+        else if (!d_base)
+            GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
+        return GJ_OK;
+    }
+    GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
+    const size_t smem = stage_bytes(sd);
+    int grid = 0;
+    GJ_TRY(grid_for(k_sorted_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));
+    k_sorted_pairs<Op><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, reinterpret_cast<uint2*>(pairs), d_base,
+                                                  d_count, pw, num_tiles);
+    GJ_CUDA_TRY(cudaGetLastError());
+    return GJ_OK;
+}
+
 // dispatch an action over the index kind
 template <class Fn>
 int with_op(const gj_index* idx, Fn&& fn) {
@@ -494,7 +684,7 @@ int with_op(const gj_index* idx, Fn&& fn) {
             return btree_dispatch(idx->bt.node_keys, [&](auto w) { return fn(op_btree<decltype(w)::value>{idx->bt}); });
         case GJ_INDEX_HARMONIA: return fn(op_harmonia{idx->hm});
         case GJ_INDEX_RADIX_SPLINE: return fn(op_rs{idx->rs});
-        case GJ_INDEX_LEARNED: return fn(op_learned{idx->ln});
+        case GJ_INDEX_LEARNED: return fn(op_learned{idx->ln, idx->ln_root});
         case GJ_INDEX_NO_OP: return fn(op_noop{});
         default: set_error("unknown index type %d", idx->type); return GJ_ERR_INVALID_ARGUMENT;
     }
@@ -503,8 +693,8 @@ int with_op(const gj_index* idx, Fn&& fn) {
 }  // namespace
 
 size_t pairs_workspace_bytes(uint64_t m) {
-    const uint64_t tiles = (m + kTile - 1) / kTile;
-    return workspace_carver::need({(size_t)(tiles ? tiles : 1) * 8, 8});
+    const uint64_t states = (m + kStateTile - 1) / kStateTile;
+    return workspace_carver::need({(size_t)(states ? states : 1) * 8, 8});
 }
 
 int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s) {
@@ -521,20 +711,28 @@ int launch_scatter_lookup(const gj_index* idx, const uint64_t* d_keys, const uin
 }
 
 int launch_pairs(const gj_index* idx, const uint64_t* d_probes, uint64_t m, const uint32_t* d_rows, uint32_t* d_pairs,
-                 const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, cudaStream_t s) {
+                 const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* d_stash,
+                 cudaStream_t s) {
     const stage_desc sd = make_stage(idx);
     return with_op(idx, [&](const auto& op) {
-        return run_pairs(op, sd, d_probes, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, s);
+        return run_pairs(op, sd, d_probes, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, d_stash, s);
+    });
+}
+
+int launch_partitioned_pairs(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
+                             uint32_t* d_pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
+                             cudaStream_t s) {
+    const stage_desc sd = make_stage(idx);
+    return with_op(idx, [&](const auto& op) {
+        return run_sorted_pairs(op, sd, d_keys, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, s);
     });
 }
 
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s) {
-    const uint32_t num_tiles = (uint32_t)((m + kTile - 1) / kTile);
-    workspace_carver wc(ws, ws_bytes);
-    wc.take<unsigned long long>(num_tiles ? num_tiles : 1);
-    unsigned int* ctr = wc.take<unsigned int>(2);
-    if (!ctr) return GJ_ERR_WORKSPACE;
-    GJ_CUDA_TRY(cudaMemcpyAsync(flag, ctr + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    pairs_ws pw;
+    size_t used = 0;
+    if (!carve_pairs_ws(ws, ws_bytes, m, &pw, &used)) return GJ_ERR_WORKSPACE;
+    GJ_CUDA_TRY(cudaMemcpyAsync(flag, pw.error, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     return GJ_OK;
 }

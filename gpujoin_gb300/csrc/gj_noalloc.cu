@@ -73,5 +73,5 @@ extern "C" int gj_inlj_pairs_noalloc(const gj_index* index, const uint64_t* d_pr
     void* scratch = nullptr;
     GJ_TRY(noalloc_scratch(&scratch));
     return gj::launch_pairs(index, d_probes, m, nullptr, d_pairs, nullptr, d_count, scratch, GJ_NOALLOC_SCRATCH_BYTES,
-                            gj::as_stream(stream));
+                            d_pairs ? d_pairs + m : nullptr, gj::as_stream(stream));
 }

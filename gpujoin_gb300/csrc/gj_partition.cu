@@ -27,6 +27,9 @@ namespace {
 
 constexpr int kPartBlock = 512;
 constexpr uint32_t kMaxRadixBits = 12;
+constexpr int kHistUnroll = 4;                                    // keys in flight per thread
+constexpr int kScatterItems = 8;                                  // keys per thread per tile
+constexpr uint32_t kScatterTile = kPartBlock * kScatterItems;     // 4096 keys
 
 __device__ __forceinline__ uint32_t part_of(uint64_t key, uint64_t min_key, uint32_t shift, uint32_t fanout) {
     if (key <= min_key) return 0;
@@ -34,18 +37,42 @@ __device__ __forceinline__ uint32_t part_of(uint64_t key, uint64_t min_key, uint
     return p >= fanout ? fanout - 1 : (uint32_t)p;
 }
 
+// sub-histograms per block: warps spread their shared-memory atomics over
+// several copies when the fanout is small (fewer same-address conflicts)
+__host__ __device__ __forceinline__ uint32_t hist_copies(uint32_t fanout) {
+    uint32_t c = 16;  // one per warp of kPartBlock
+    while (c > 1 && (size_t)c * fanout * sizeof(uint32_t) > 32768) c >>= 1;
+    return c;
+}
+
 // hist[p * G + b] = number of keys of block b's chunk in partition p
 __global__ void __launch_bounds__(kPartBlock) k_part_hist(const uint64_t* __restrict__ keys, uint64_t m, uint64_t chunk,
                                                           uint64_t min_key, uint32_t shift, uint32_t fanout,
                                                           uint64_t* __restrict__ hist) {
     extern __shared__ uint32_t s_hist[];
-    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_hist[p] = 0;
+    const uint32_t copies = hist_copies(fanout);
+    for (uint32_t p = threadIdx.x; p < fanout * copies; p += blockDim.x) s_hist[p] = 0;
     __syncthreads();
+    uint32_t* mine = s_hist + ((threadIdx.x >> 5) & (copies - 1)) * fanout;
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-        atomicAdd(&s_hist[part_of(__ldg(reinterpret_cast<const unsigned long long*>(keys) + i), min_key, shift, fanout)], 1u);
+    const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += (uint64_t)kPartBlock * kHistUnroll) {
+        uint64_t k[kHistUnroll];
+#pragma unroll
+        for (int u = 0; u < kHistUnroll; ++u) {
+            const uint64_t j = i + (uint64_t)u * kPartBlock;
+            k[u] = j < b1 ? __ldcs(k64 + j) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < kHistUnroll; ++u)
+            if (i + (uint64_t)u * kPartBlock < b1) atomicAdd(&mine[part_of(k[u], min_key, shift, fanout)], 1u);
+    }
     __syncthreads();
-    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) hist[(uint64_t)p * gridDim.x + blockIdx.x] = s_hist[p];
+    for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) {
+        uint32_t c = 0;
+        for (uint32_t q = 0; q < copies; ++q) c += s_hist[q * fanout + p];
+        hist[(uint64_t)p * gridDim.x + blockIdx.x] = c;
+    }
 }
 
 // offsets[p] = start of partition p (inclusive scan of hist, read at the
@@ -56,30 +83,116 @@ __global__ void k_part_offsets(const uint64_t* __restrict__ incl, uint32_t fanou
         offsets[p] = p == 0 ? 0 : (p == fanout ? m : incl[(uint64_t)p * nblocks - 1]);
 }
 
-// scatter block b's chunk.  The flat (partition, block) order of the scanned
+// out[p] = sum of in[0..p) over count entries, by the whole block
+__device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t count) {
+    __shared__ uint32_t s_warp[kPartBlock / 32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t per = (count + kPartBlock - 1) / kPartBlock;
+    const uint32_t begin = threadIdx.x * per;
+    uint32_t sum = 0;
+    for (uint32_t q = 0; q < per; ++q)
+        if (begin + q < count) sum += in[begin + q];
+    uint32_t incl = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (uint32_t)d) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int kWarps = kPartBlock / 32;
+        const uint32_t v = lane < kWarps ? s_warp[lane] : 0u;
+        uint32_t w = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= (uint32_t)d) w += t;
+        }
+        if (lane < kWarps) s_warp[lane] = w - v;
+    }
+    __syncthreads();
+    uint32_t run = s_warp[warp] + incl - sum;
+    for (uint32_t q = 0; q < per; ++q)
+        if (begin + q < count) {
+            out[begin + q] = run;
+            run += in[begin + q];
+        }
+}
+
+// Scatter block b's chunk.  The flat (partition, block) order of the scanned
 // histogram makes the start of cell c the inclusive sum of cell c - 1, so the
-// keys are read once.  Ranks inside a block come from shared-memory atomics:
-// the order inside a partition follows the block order, not the probe order
-// within one block.
-__global__ void __launch_bounds__(kPartBlock) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
+// keys are read once.  Each tile of kScatterTile keys is first grouped by
+// partition in shared memory (a counting sort whose ranks come from
+// shared-memory atomics), then every partition's run of the tile is written
+// with consecutive threads on consecutive addresses: whole sectors instead of
+// one scattered 8-byte store per key.  The order inside a partition follows
+// the block and tile order; inside a tile it is not fixed.
+// 3 resident blocks (42 registers, about 52 KB of shared memory each for
+// fanouts up to 2^8)
+__global__ void __launch_bounds__(kPartBlock, 3) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
                                                              uint64_t chunk, uint64_t min_key, uint32_t shift,
                                                              uint32_t fanout, const uint64_t* __restrict__ incl,
                                                              uint64_t row_base, uint64_t* __restrict__ out_keys,
                                                              uint32_t* __restrict__ out_rows) {
-    extern __shared__ unsigned long long s_next[];
+    extern __shared__ unsigned long long s_mem[];
+    uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_mem);                       // kScatterTile
+    unsigned long long* s_dst = s_mem + kScatterTile;                            // fanout: next output slot
+    uint32_t* s_rows = reinterpret_cast<uint32_t*>(s_dst + fanout);              // kScatterTile
+    uint32_t* s_cnt = s_rows + kScatterTile;                                     // fanout
+    uint32_t* s_start = s_cnt + fanout;                                          // fanout
     for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) {
         const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
-        s_next[p] = cell == 0 ? 0ull : incl[cell - 1];
+        s_dst[p] = cell == 0 ? 0ull : incl[cell - 1];
     }
-    __syncthreads();
+    const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        const uint64_t k = __ldcs(reinterpret_cast<const unsigned long long*>(keys) + i);
-        const uint32_t p = part_of(k, min_key, shift, fanout);
-        const unsigned long long d = atomicAdd(&s_next[p], 1ull);
-        out_keys[d] = k;
-        out_rows[d] = (uint32_t)(row_base + i);
+    for (uint64_t t0 = b0; t0 < b1; t0 += kScatterTile) {
+        const uint32_t tn = b1 - t0 < kScatterTile ? (uint32_t)(b1 - t0) : kScatterTile;
+        for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_cnt[p] = 0;
+        __syncthreads();
+        uint64_t key[kScatterItems];
+        uint32_t slot[kScatterItems];  // partition << 13 | rank inside the tile's partition run
+        static_assert(kScatterTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
+#pragma unroll
+        for (int k = 0; k < kScatterItems; ++k) {
+            const uint32_t j = k * kPartBlock + threadIdx.x;
+            key[k] = j < tn ? __ldcs(k64 + t0 + j) : 0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < kScatterItems; ++k) {
+            const uint32_t j = k * kPartBlock + threadIdx.x;
+            const uint32_t p = part_of(key[k], min_key, shift, fanout);
+            slot[k] = j < tn ? (p << 13) | atomicAdd(&s_cnt[p], 1u) : 0u;
+        }
+        __syncthreads();
+        block_exclusive_scan(s_cnt, s_start, fanout);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kScatterItems; ++k) {
+            const uint32_t j = k * kPartBlock + threadIdx.x;
+            if (j < tn) {
+                const uint32_t q = s_start[slot[k] >> 13] + (slot[k] & ((1u << 13) - 1));
+                s_keys[q] = key[k];
+                s_rows[q] = (uint32_t)(row_base + t0 + j);
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < tn; j += kPartBlock) {
+            const uint64_t k = s_keys[j];
+            const uint32_t p = part_of(k, min_key, shift, fanout);
+            const uint64_t d = s_dst[p] + (j - s_start[p]);
+            __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
+            __stcg(out_rows + d, s_rows[j]);
+        }
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_dst[p] += s_cnt[p];
+        __syncthreads();
     }
+}
+
+size_t scatter_smem_bytes(uint32_t fanout) {
+    return (size_t)kScatterTile * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)fanout * (8 + 4 + 4);
 }
 
 struct partition_plan {
@@ -90,7 +203,7 @@ struct partition_plan {
 partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
     partition_plan pl;
     pl.fanout = 1u << radix_bits;
-    uint64_t nb = (uint64_t)sm_count * 2;
+    uint64_t nb = (uint64_t)sm_count * 3;  // the scatter kernel keeps 3 blocks per SM
     const uint64_t min_chunk = 4096;
     if (nb * min_chunk > m) nb = std::max<uint64_t>(1, (m + min_chunk - 1) / min_chunk);
     pl.chunk = (m + nb - 1) / nb;
@@ -124,8 +237,8 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
         if (d_offsets) GJ_CUDA_TRY(cudaMemsetAsync(d_offsets, 0, ((size_t)pl.fanout + 1) * sizeof(uint64_t), s));
         return GJ_OK;
     }
-    const size_t smem_hist = pl.fanout * sizeof(uint32_t);
-    const size_t smem_scatter = pl.fanout * sizeof(unsigned long long);
+    const size_t smem_hist = (size_t)pl.fanout * hist_copies(pl.fanout) * sizeof(uint32_t);
+    const size_t smem_scatter = scatter_smem_bytes(pl.fanout);
     if (smem_scatter > 48 * 1024)
         GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_scatter));
     k_part_hist<<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
@@ -264,7 +377,8 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
         GJ_TRY(range_partition_impl(d_probes + off, len, min_key, shift, radix_bits, off, pkeys, prows, nullptr, pws,
                                     pws_bytes, s));
         if (d_positions) GJ_TRY(launch_scatter_lookup(index, pkeys, prows, len, d_positions, s));
-        if (d_pairs) GJ_TRY(launch_pairs(index, pkeys, len, prows, d_pairs, d_count, d_count, qws, qws_bytes, s));
+        if (d_pairs)
+            GJ_TRY(launch_partitioned_pairs(index, pkeys, prows, len, d_pairs, d_count, d_count, qws, qws_bytes, s));
     }
     return GJ_OK;
 }

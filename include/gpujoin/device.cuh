@@ -364,7 +364,16 @@ struct learned_leaf {
     float slope;      // positions per unit key distance
     uint32_t err_lo;
     uint32_t err_hi;
+    uint64_t pad;     // one 32-byte sector per leaf: a single load
 };
+static_assert(sizeof(learned_leaf) == 32, "a leaf is one sector");
+
+// The root MLP is always evaluated 32 wide: 1 -> 32 -> 32 -> 1 with ReLU over
+// [W1(32) b1(32) W2(32x32, out-major) b2(32) W3(32) b3].  Narrower trained
+// networks are stored zero-padded; the padding adds exact zeros, so the
+// result is the narrower network's.
+constexpr int kMlpWidth = 32;
+constexpr int kMlpParams = 2 * kMlpWidth + kMlpWidth * kMlpWidth + 2 * kMlpWidth + 1;  // 1153
 
 struct learned_view {
     const uint64_t* col;
@@ -373,34 +382,34 @@ struct learned_view {
     float inv_range;            // 1 / (max_key - min_key) (0 if the range is empty)
     uint32_t num_leaves;
     uint32_t root_kind;         // GJ_LEARNED_ROOT_LINEAR or GJ_LEARNED_ROOT_MLP
-    uint32_t hidden;            // MLP width H (<= 32)
-    const float* root;          // [a, b] (linear) or MLP parameters [W1 b1 W2 b2 W3 b3]
-    const learned_leaf* leaves;
+    uint32_t hidden;            // trained MLP width H (<= 32), stored padded to 32
+    const float* root;          // [a, b] (linear) or kMlpParams MLP parameters
+    const learned_leaf* leaves; // 32-byte aligned
     uint32_t col_aligned;       // column base is 32-byte aligned
     uint32_t pad;
 };
 
-// root MLP 1 -> H -> H -> 1 with ReLU, parameters [W1(H) b1(H) W2(HxH, out-major) b2(H) W3(H) b3]
-GJ_DEVICE_INLINE float mlp_forward(const float* P, int H, float x) {
-    const float* W1 = P;
-    const float* b1 = P + H;
-    const float* W2 = P + 2 * H;
-    const float* b2 = W2 + H * H;
-    const float* W3 = b2 + H;
-    float h1[32];
+// root parameters carried by value (a kernel argument): the forward pass then
+// reads its weights as constant-bank operands of its FMAs
+struct learned_root_params {
+    float w[kMlpParams];
+};
+
+GJ_DEVICE_INLINE float mlp32_forward(const float* P, float x) {
+    constexpr int H = kMlpWidth;
+    float h1[H];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const float a = (j < H) ? fmaf(W1[j], x, b1[j]) : 0.f;
+    for (int j = 0; j < H; ++j) {
+        const float a = fmaf(P[j], x, P[H + j]);
         h1[j] = a > 0.f ? a : 0.f;
     }
-    float out = W3[H];  // b3 directly follows W3
-    for (int o = 0; o < H; ++o) {
-        const float* w = W2 + o * H;
-        float a = b2[o];
+    float out = P[4 * H + H * H];  // b3
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if (j < H) a = fmaf(w[j], h1[j], a);
-        out = fmaf(W3[o], a > 0.f ? a : 0.f, out);
+    for (int o = 0; o < H; ++o) {
+        float a = P[2 * H + H * H + o];  // b2[o]
+#pragma unroll
+        for (int j = 0; j < H; ++j) a = fmaf(P[2 * H + o * H + j], h1[j], a);
+        out = fmaf(P[3 * H + H * H + o], a > 0.f ? a : 0.f, out);
     }
     return out;
 }
@@ -412,8 +421,7 @@ GJ_DEVICE_INLINE float learned_norm(const learned_view& v, uint64_t key) {
 }
 
 GJ_DEVICE_INLINE uint32_t learned_route(const learned_view& v, const float* root, float x) {
-    const float r = (v.root_kind == GJ_LEARNED_ROOT_MLP) ? mlp_forward(root, (int)v.hidden, x)
-                                                         : fmaf(root[0], x, root[1]);
+    const float r = (v.root_kind == GJ_LEARNED_ROOT_MLP) ? mlp32_forward(root, x) : fmaf(root[0], x, root[1]);
     const float lf = floorf(r * (float)v.num_leaves);
     if (!(lf > 0.f)) return 0;  // also catches NaN
     if (lf >= (float)v.num_leaves) return v.num_leaves - 1;
@@ -431,14 +439,14 @@ GJ_DEVICE_INLINE int64_t learned_predict(const learned_leaf& lf, uint64_t key) {
 
 GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* root, uint64_t key) {
     const uint32_t li = learned_route(v, root, learned_norm(v, key));
-    const uint64_t* lp = reinterpret_cast<const uint64_t*>(v.leaves + li);
+    uint64_t w[4];
+    ld_sector(reinterpret_cast<const uint64_t*>(v.leaves + li), w);
     learned_leaf lf;
-    lf.x0 = ld_ro(lp);
-    const uint64_t w1 = ld_ro(lp + 1), w2 = ld_ro(lp + 2);
-    lf.base = (uint32_t)w1;
-    lf.slope = __uint_as_float((uint32_t)(w1 >> 32));
-    lf.err_lo = (uint32_t)w2;
-    lf.err_hi = (uint32_t)(w2 >> 32);
+    lf.x0 = w[0];
+    lf.base = (uint32_t)w[1];
+    lf.slope = __uint_as_float((uint32_t)(w[1] >> 32));
+    lf.err_lo = (uint32_t)w[2];
+    lf.err_hi = (uint32_t)(w[2] >> 32);
     const int64_t pred = learned_predict(lf, key);
     const int64_t n = (int64_t)v.n;
     // window [pred - err_lo, pred + err_hi + 1) clamped to [0, n]; a probe far

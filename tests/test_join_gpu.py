@@ -117,8 +117,35 @@ def test_partitioned_inlj_fanouts(orc, gj, cuda, bits):
     col = column(rng, 1 << 18)
     pr = probes_for(rng, col, 200000)
     ix = gj.btree_index().construct(None, to_dev(torch, col))
-    pos, _, _ = ix.partitioned_inlj(to_dev(torch, pr), radix_bits=bits)
-    np.testing.assert_array_equal(from_dev_u32(pos), orc.exact_lookup(col, pr))
+    pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), radix_bits=bits, pairs=True)
+    exp = orc.exact_lookup(col, pr)
+    np.testing.assert_array_equal(from_dev_u32(pos), exp)
+    rows, bpos = pairs_of(prs, cnt)
+    erows, epos = orc.pairs_from_positions(exp)
+    order = np.argsort(rows, kind="stable")
+    np.testing.assert_array_equal(rows[order], erows)
+    np.testing.assert_array_equal(bpos[order], epos)
+
+
+@pytest.mark.parametrize("kind", ["btree", "harmonia", "radix_spline", "binary_search", "learned"])
+def test_partitioned_pairs_sorted_tiles(orc, gj, cuda, kind):
+    # tiles of equal keys, a tile spanning the whole key range, many windows
+    import torch
+
+    rng = np.random.default_rng(99)
+    col = column(rng, 32 * 20000)
+    pr = np.concatenate([np.full(5000, col[777], dtype=np.uint64), probes_for(rng, col, 300000),
+                         np.array([0, (1 << 64) - 1], dtype=np.uint64), np.full(3000, col[-1], dtype=np.uint64)])
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    exp = expected(orc, kind, col, pr)
+    erows, epos = orc.pairs_from_positions(exp)
+    for window, bits in ((len(pr), 8), (70001, 10), (4096, 12)):
+        _, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=bits, positions=False,
+                                          pairs=True)
+        rows, bpos = pairs_of(prs, cnt)
+        order = np.argsort(rows, kind="stable")
+        np.testing.assert_array_equal(rows[order], erows, err_msg=f"{kind} window {window}")
+        np.testing.assert_array_equal(bpos[order], epos, err_msg=f"{kind} window {window}")
 
 
 def star_inputs(rng, nfact, ndim):
