@@ -391,28 +391,9 @@ def partitioned_workload(args, world, rank, device, stream):
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
 
-    # autotune fanout and window on a sample of the probes
-    sample = probes[: 1 << min(m_log2, 25)]
-    best = None
-    tune = {}
-    for bits in (8, 10, 12):
-        for window in (sample.numel(), sample.numel() // 4):
-            need = ctypes.c_size_t()
-            gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
-            ws = torch.empty(need.value, dtype=torch.uint8, device=device)
-
-            def run():
-                gj._check(gj.lib().gj_partitioned_inlj(ix.handle, sample.data_ptr(), sample.numel(), window, bits,
-                                                        None, pairs.data_ptr(), count.data_ptr(), ws.data_ptr(),
-                                                        ws.numel(), stream.cuda_stream))
-
-            t = time_steps(run, 2, 1, stream, 1, device) / 2
-            tune[f"bits{bits}_window{window}"] = round(t, 3)
-            if best is None or t < best[0]:
-                best = (t, bits, window / sample.numel())
-            del ws
-    _, bits, wfrac = best
-    window = max(1, int(m * wfrac))
+    # fanout and window from the library's autotuner, on the same probes
+    bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
+    tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3)}
     need = ctypes.c_size_t()
     gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
     ws = torch.empty(need.value, dtype=torch.uint8, device=device)
@@ -446,7 +427,7 @@ def partitioned_workload(args, world, rank, device, stream):
         world * m * args.steps / (ms / 1e3), "probe tuples/s", per_step,
         f"partitioned INLJ: {n} uniform uint64 keys (2^{n_log2}), {m} Zipf({args.theta}) probes (2^{m_log2}), "
         f"{ix.type_name()}, range partition 2^{bits}, window {window}",
-        {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune_ms": tune,
+        {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune": tune,
                          "plain_pairs_ms_per_step": plain_ms,
                          "plain_pairs_tuples_per_s": m / (plain_ms / 1e3)},
          "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -564,9 +545,11 @@ def learned_workload(args, world, rank, device, stream):
 
 def batch_workload(args, world, rank, device, stream):
     """Batched lookup stream: 8 indexes (B+tree, Harmonia, RadixSpline,
-    learned; 2^20..2^27 keys), 4096 batches of lognormal size in [1k, 16M]
-    drawn Zipf(0.8) against their index, admitted in rounds by an HBM budget;
-    one persistent kernel against one launch per batch."""
+    learned; 2^20..2^27 uniform or lognormal keys), 4096 batches of lognormal
+    size in [1k, 16M] drawn Zipf(0.8) against their index, admitted in rounds
+    by an HBM budget.  Each round is a plan run as one persistent kernel
+    replayed from a CUDA graph (tile shape autotuned on the first round),
+    against the same batches issued one kernel launch at a time."""
     import numpy as np
     import torch
 
@@ -595,58 +578,53 @@ def batch_workload(args, world, rank, device, stream):
     max_round = max(int(sizes[r].sum()) for r in rounds)
     probes = torch.empty(max_round, dtype=torch.int64, device=device)
     out = torch.empty(max_round, dtype=torch.int32, device=device)
-    done = torch.zeros(nb, dtype=torch.int64, device=device)
-    import ctypes
-    need = ctypes.c_size_t()
-    gj.lib().gj_batch_workspace_size(len(indexes), nb, ctypes.byref(need))
-    ws = torch.empty(need.value, dtype=torch.uint8, device=device)
+    done = torch.zeros(nb + 1, dtype=torch.int64, device=device)
     total = int(sizes.sum())
-    res = {}
-    for mode in (0, 1):
-        lat = []
-        t_all = 0.0
-        for r in rounds:
-            bs = sizes[r]
-            offs = np.concatenate([[0], np.cumsum(bs)[:-1]]).astype(np.uint64)
-            for j, b in enumerate(r):
-                probes[int(offs[j]): int(offs[j] + bs[j])] = gj.generate_probes(cols[which[b]], int(bs[j]), theta=0.8,
-                                                                       seed=args.seed + int(b))
-            start_ev = torch.cuda.Event(enable_timing=True)
-            end_ev = torch.cuda.Event(enable_timing=True)
+    tiles = None
+    res = {"persistent_graph": {"ms": 0.0, "lat": []}, "per_launch": {"ms": 0.0, "lat": []}}
+    launches = 0
+    for ri, r in enumerate(rounds):
+        bs = sizes[r]
+        offs = np.concatenate([[0], np.cumsum(bs)[:-1]]).astype(np.uint64)
+        for j, b in enumerate(r):
+            probes[int(offs[j]): int(offs[j] + bs[j])] = gj.generate_probes(cols[which[b]], int(bs[j]), theta=0.8,
+                                                                           seed=args.seed + int(b))
+        plan = gj.batch_plan(indexes, which[r], offs, bs, tile_items=tiles or 0)
+        if tiles is None:
+            tiles, _ = plan.autotune(probes, out)
+        for key, mode, graph in (("persistent_graph", 0, True), ("per_launch", 1, False)):
+            run = plan.run_graph if graph else plan.run
+            d = done[: len(r) + 1]
+            for _ in range(max(1, args.warmup)):
+                run(probes, out, mode, d)
             torch.cuda.synchronize()
-            t0 = torch.cuda.Event(enable_timing=True)
-
-            def run():
-                gj.batch_lookup(indexes, which[r], offs, bs, probes, out, mode=mode, d_done_ns=done[: len(r)],
-                                workspace=ws)
-
-            run()  # warm
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run(probes, out, mode, d)
+            e1.record(stream)
             torch.cuda.synchronize()
-            start_ns = None
-            start_ev.record(stream)
-            stamp = torch.zeros(1, dtype=torch.int64, device=device)
-            run()
-            end_ev.record(stream)
-            torch.cuda.synchronize()
-            t_all += start_ev.elapsed_time(end_ev)
-            d = done[: len(r)].cpu().numpy().astype(np.int64)
-            lat.extend(((d - d.min()) / 1e3 + 0.0).tolist())
-        lat = np.array(lat)
-        res["persistent" if mode == 0 else "per_launch"] = {
-            "tuples_per_s": total / (t_all / 1e3), "ms_total": t_all,
-            "p50_batch_completion_us": float(np.percentile(lat, 50)),
-            "p99_batch_completion_us": float(np.percentile(lat, 99))}
-    head = res["persistent"]
+            res[key]["ms"] += e0.elapsed_time(e1)
+            t = d.cpu().numpy().astype(np.int64)
+            res[key]["lat"].extend(((t[: len(r)] - t[len(r)]) / 1e3).tolist())
+            launches += 1 if mode == 0 else len(r)
+        plan.free()
+    summary = {}
+    for key, v in res.items():
+        lat = np.array(v["lat"])
+        summary[key] = {"tuples_per_s": total / (v["ms"] / 1e3), "ms_total": round(v["ms"], 3),
+                        "p50_batch_latency_us": round(float(np.percentile(lat, 50)), 1),
+                        "p99_batch_latency_us": round(float(np.percentile(lat, 99)), 1)}
+    summary["tile_items"] = tiles
+    summary["rounds"] = len(rounds)
+    head = summary["persistent_graph"]
     return _base_line(
         args, world, "batched lookup stream probe tuples/s (1 GB300 per rank)", world * head["tuples_per_s"],
         "probe tuples/s", head["ms_total"],
-        f"batched stream: 8 indexes (2^20..2^27 keys), {nb} batches, {total} probes, {len(rounds)} admission rounds",
-        {"batch": res, "roofline": None, "gpu_launches": len(rounds), "cpu_baseline": None, "e2e": None})
+        f"batched stream: 8 indexes (2^20..2^27 keys), {nb} batches, {total} probes, {len(rounds)} admission rounds "
+        f"of <= 2 GiB of probes; latency = batch completion - round start",
+        {"batch": summary, "roofline": None, "gpu_launches": launches, "cpu_baseline": None, "e2e": None})
 
 
-# ---------------------------------------------------------------------------
-# reference arm: the reference's CPU lookup path on the host cores
-# ---------------------------------------------------------------------------
 def reference_main(args):
     import numpy as np
 

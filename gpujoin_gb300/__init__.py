@@ -114,8 +114,16 @@ _SIGNATURES = {
     "gj_partitioned_inlj": (_i32, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_star_join_sum": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
     "gj_learned_mlp_grad": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
-    "gj_batch_lookup": (_i32, [ctypes.POINTER(_vp), _u32, _vp, _vp, _vp, _u32, _vp, _vp, _u32, _vp, _vp, _sz, _vp]),
-    "gj_batch_workspace_size": (_i32, [_u32, _u32, ctypes.POINTER(_sz)]),
+    "gj_autotune_partitioned": (_i32, [_vp, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u64),
+                                       ctypes.POINTER(ctypes.c_float)]),
+    "gj_autotune_btree": (_i32, [_vp, _u64, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
+                                 ctypes.POINTER(ctypes.c_float)]),
+    "gj_batch_plan_create": (_i32, [ctypes.POINTER(_vp), _u32, _vp, _vp, _vp, _u32, _u32, _vp, ctypes.POINTER(_vp)]),
+    "gj_batch_plan_free": (_i32, [_vp]),
+    "gj_batch_plan_tile_items": (_i32, [_vp, ctypes.POINTER(_u32)]),
+    "gj_batch_plan_run": (_i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
+    "gj_batch_plan_run_graph": (_i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
+    "gj_batch_plan_autotune": (_i32, [_vp, _vp, _vp, _vp, ctypes.POINTER(_u32), ctypes.POINTER(ctypes.c_float)]),
     "gj_generate_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_generate_sorted_keys": (_i32, [_vp, _u64, _u32, _u64, _u64, _vp, _sz, _vp]),
     "gj_generate_probes": (_i32, [_vp, _u64, _vp, _u64, ctypes.c_double, ctypes.c_double, _u64, _vp]),
@@ -460,25 +468,85 @@ def learned_mlp_grad(d_params, hidden: int, d_x, d_y, stream=None):
 # --------------------------------------------------------------------------
 # batched lookup stream
 # --------------------------------------------------------------------------
-def batch_lookup(indexes, batch_index, probe_offset, batch_size, d_probes, d_positions, mode: int = 0,
-                 d_done_ns=None, workspace=None, stream=None):
-    """Many probe batches against several indexes; mode 0 = one persistent kernel, 1 = one launch per batch."""
-    import numpy as np
+def autotune_partitioned(index, d_probes, stream=None):
+    """Fastest (radix_bits, window_size, ms) of the partitioned INLJ on these probes."""
+    bits, window, ms = _u32(0), _u64(0), ctypes.c_float(0)
+    _check(lib().gj_autotune_partitioned(index.handle, _ptr(d_probes), d_probes.numel(), _stream(stream),
+                                         ctypes.byref(bits), ctypes.byref(window), ctypes.byref(ms)))
+    return bits.value, window.value, ms.value
 
-    nb = len(batch_index)
-    arr_t = _vp * len(indexes)
-    handles = arr_t(*[ix.handle for ix in indexes])
-    bi = np.ascontiguousarray(batch_index, dtype=np.uint32)
-    po = np.ascontiguousarray(probe_offset, dtype=np.uint64)
-    bs = np.ascontiguousarray(batch_size, dtype=np.uint64)
-    dev = d_probes.device
-    if workspace is None:
-        need = _sz(0)
-        _check(lib().gj_batch_workspace_size(len(indexes), nb, ctypes.byref(need)))
-        workspace = _workspace(need.value, dev)
-    _check(lib().gj_batch_lookup(handles, len(indexes), bi.ctypes.data, po.ctypes.data, bs.ctypes.data, nb,
-                                 _ptr(d_probes), _ptr(d_positions), mode, _ptr(d_done_ns), _ptr(workspace),
-                                 workspace.numel(), _stream(stream)))
+
+def autotune_btree(d_keys, d_probes, stream=None):
+    """Fastest (node_keys, leaf_keys, ms) of B+tree lookups of these probes into these keys."""
+    w, l, ms = _u32(0), _u32(0), ctypes.c_float(0)
+    _check(lib().gj_autotune_btree(_ptr(d_keys), d_keys.numel(), _ptr(d_probes), d_probes.numel(), _stream(stream),
+                                   ctypes.byref(w), ctypes.byref(l), ctypes.byref(ms)))
+    return w.value, l.value, ms.value
+
+
+class batch_plan:
+    """Plan of a batched lookup stream: many probe batches against several
+    indexes, descriptors uploaded once.  run() enqueues one persistent kernel
+    (mode 0) or one launch per batch (mode 1); run_graph() replays the run
+    through a CUDA graph the plan captures; autotune() picks the tile shape."""
+
+    def __init__(self, indexes, batch_index, probe_offset, batch_size, tile_items: int = 0, stream=None):
+        import numpy as np
+
+        self.indexes = list(indexes)  # the plan refers to them: keep them alive
+        arr_t = _vp * len(self.indexes)
+        handles = arr_t(*[ix.handle for ix in self.indexes])
+        self._bi = np.ascontiguousarray(batch_index, dtype=np.uint32)
+        self._po = np.ascontiguousarray(probe_offset, dtype=np.uint64)
+        self._bs = np.ascontiguousarray(batch_size, dtype=np.uint64)
+        self.num_batches = len(self._bi)
+        out = _vp()
+        _check(lib().gj_batch_plan_create(handles, len(self.indexes), self._bi.ctypes.data, self._po.ctypes.data,
+                                          self._bs.ctypes.data, self.num_batches, tile_items, _stream(stream),
+                                          ctypes.byref(out)))
+        self._plan = out
+
+    @property
+    def tile_items(self) -> int:
+        v = _u32(0)
+        _check(lib().gj_batch_plan_tile_items(self._plan, ctypes.byref(v)))
+        return v.value
+
+    def run(self, d_probes, d_positions, mode: int = 0, d_done_ns=None, stream=None):
+        _check(lib().gj_batch_plan_run(self._plan, _ptr(d_probes), _ptr(d_positions), mode, _ptr(d_done_ns),
+                                       _stream(stream)))
+        return d_positions
+
+    def run_graph(self, d_probes, d_positions, mode: int = 0, d_done_ns=None, stream=None):
+        _check(lib().gj_batch_plan_run_graph(self._plan, _ptr(d_probes), _ptr(d_positions), mode, _ptr(d_done_ns),
+                                             _stream(stream)))
+        return d_positions
+
+    def autotune(self, d_probes, d_positions, stream=None):
+        items, ms = _u32(0), ctypes.c_float(0)
+        _check(lib().gj_batch_plan_autotune(self._plan, _ptr(d_probes), _ptr(d_positions), _stream(stream),
+                                            ctypes.byref(items), ctypes.byref(ms)))
+        return items.value, ms.value
+
+    def free(self) -> None:
+        if getattr(self, "_plan", None) is not None and self._plan.value:
+            _check(lib().gj_batch_plan_free(self._plan))
+            self._plan = _vp(None)
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def batch_lookup(indexes, batch_index, probe_offset, batch_size, d_probes, d_positions, mode: int = 0,
+                 d_done_ns=None, graph: bool = False, stream=None):
+    """One-shot batched lookup (plan, run, free); mode 0 = persistent kernel, 1 = one launch per batch."""
+    plan = batch_plan(indexes, batch_index, probe_offset, batch_size, stream=stream)
+    (plan.run_graph if graph else plan.run)(d_probes, d_positions, mode, d_done_ns, stream)
+    _torch().cuda.synchronize(d_probes.device)
+    plan.free()
     return d_positions
 
 

@@ -2,18 +2,27 @@
 // against several indexes.  Not in the reference (its driver runs one index
 // and one probe column per process, src/index_lookup_new.cu:375-434).
 //
-// mode 0: one persistent kernel.  All batches are cut into tiles; blocks
-//         claim tiles in order from an atomic counter (largest-first order is
-//         the caller's choice of batch order), so small batches never wait
-//         behind a kernel boundary and no SM idles at batch tails.
+// A plan (gj_batch_plan) holds the batch descriptors, the index views and a
+// tile -> batch map in device memory, uploaded once when the plan is made.
+// Running a plan only enqueues device work on the caller's stream -- a memset
+// and kernels, no host synchronisation and no allocation -- so it can be
+// captured in a CUDA graph; the plan captures and replays one itself
+// (gj_batch_plan_run_graph).
+//
+// mode 0: one persistent kernel.  All batches are cut into tiles of
+//         kBatchBlock * tile_items probes; blocks claim tiles in order from an
+//         atomic counter, so small batches never wait behind a kernel
+//         boundary and no SM idles at batch tails.
 // mode 1: one lookup launch per batch -- the baseline the persistent kernel
 //         is measured against.
 // Both modes can record per-batch completion times (device globaltimer) for
-// latency percentiles.
+// latency percentiles.  The tile shape is the plan's autotuned parameter.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <cstring>
+#include <new>
+#include <type_traits>
 #include <vector>
 
 #include "gj_internal.h"
@@ -22,8 +31,6 @@ namespace gj {
 namespace {
 
 constexpr int kBatchBlock = 256;
-constexpr int kBatchItems = 8;
-constexpr uint64_t kBatchTile = (uint64_t)kBatchBlock * kBatchItems;
 
 struct any_view {
     int32_t type;
@@ -36,11 +43,12 @@ struct any_view {
         learned_view ln;
     } u;
 };
+static_assert(sizeof(any_view) % 4 == 0, "views are staged as 32-bit words");
 
 struct batch_desc {
     uint64_t offset;      // first probe of the batch
     uint64_t size;        // probes in the batch
-    uint64_t tile_begin;  // first global tile of the batch
+    uint64_t tile_begin;  // first tile of the batch
     uint32_t index;       // view of the batch
     uint32_t pad;
 };
@@ -51,13 +59,9 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
-__device__ __forceinline__ uint32_t any_lookup(const any_view& v, uint64_t key) {
+__device__ __forceinline__ uint32_t any_lookup(const any_view& v, const float* root, uint64_t key) {
     switch (v.type) {
-        case GJ_INDEX_BINARY_SEARCH: {
-            bs_view b = v.u.bs;
-            b.fence_slots = 0;
-            return bs_lookup(b, nullptr, key);
-        }
+        case GJ_INDEX_BINARY_SEARCH: return bs_lookup(v.u.bs, nullptr, key);
         case GJ_INDEX_BTREE:
             switch (v.u.bt.node_keys) {
                 case 4: return btree_lookup<4>(v.u.bt, nullptr, key);
@@ -68,53 +72,64 @@ __device__ __forceinline__ uint32_t any_lookup(const any_view& v, uint64_t key) 
             }
         case GJ_INDEX_HARMONIA: return harmonia_lookup(v.u.hm, nullptr, key);
         case GJ_INDEX_RADIX_SPLINE: return rs_lookup(v.u.rs, key);
-        case GJ_INDEX_LEARNED: return learned_lookup(v.u.ln, v.u.ln.root, key);
+        case GJ_INDEX_LEARNED: return learned_lookup(v.u.ln, root, key);
         default: return kInvalid;
     }
 }
 
+// The block stages the view of its tile's index (and a learned index's root
+// parameters) in shared memory; consecutive tiles of one batch reuse them.
+template <int kItems>
 __global__ void __launch_bounds__(kBatchBlock) k_batch(const any_view* __restrict__ views,
-                                                       const batch_desc* __restrict__ batches, uint32_t nb,
-                                                       uint64_t total_tiles, const uint64_t* __restrict__ probes,
+                                                       const batch_desc* __restrict__ batches,
+                                                       const uint32_t* __restrict__ tile_batch, uint32_t total_tiles,
+                                                       const uint64_t* __restrict__ probes,
                                                        uint32_t* __restrict__ out, unsigned int* tile_counter,
                                                        unsigned long long* remaining, uint64_t* done_ns) {
-    __shared__ uint32_t s_tile;
-    __shared__ any_view s_view;
-    __shared__ uint32_t s_batch;
+    constexpr uint64_t kTile = (uint64_t)kBatchBlock * kItems;
+    __shared__ uint32_t s_tile, s_batch;
+    __shared__ __align__(16) any_view s_view;
+    __shared__ float s_root[kMlpParams];
+    uint32_t staged = 0xFFFFFFFFu;  // index whose view is in shared memory
     for (;;) {
         if (threadIdx.x == 0) {
             const uint32_t t = atomicAdd(tile_counter, 1u);
             s_tile = t;
-            if (t < total_tiles) {
-                // batch owning tile t: last b with tile_begin <= t
-                uint32_t lo = 0, hi = nb;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (batches[mid].tile_begin <= t) lo = mid; else hi = mid;
-                }
-                s_batch = lo;
-            }
+            if (t < total_tiles) s_batch = tile_batch[t];
         }
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= total_tiles) break;
-        const uint32_t b = s_batch;
-        if (threadIdx.x == 0) s_view = views[batches[b].index];
-        __syncthreads();
-        const batch_desc bd = batches[b];
-        const uint64_t first = (tile - bd.tile_begin) * kBatchTile;
-        const uint64_t last = min(bd.size, first + kBatchTile);
-        for (uint64_t j = first + threadIdx.x; j < last; j += kBatchBlock) {
-            const uint64_t i = bd.offset + j;
-            const uint64_t key = __ldcs(reinterpret_cast<const unsigned long long*>(probes + i));
-            __stcs(out + i, any_lookup(s_view, key));
+        const batch_desc bd = batches[s_batch];
+        if (bd.index != staged) {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(views + bd.index);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_view);
+            for (uint32_t w = threadIdx.x; w < sizeof(any_view) / 4; w += kBatchBlock) dst[w] = src[w];
+            __syncthreads();
+            if (s_view.type == GJ_INDEX_LEARNED) {
+                const uint32_t np = s_view.u.ln.root_kind == GJ_LEARNED_ROOT_MLP ? (uint32_t)kMlpParams : 2u;
+                for (uint32_t w = threadIdx.x; w < np; w += kBatchBlock) s_root[w] = s_view.u.ln.root[w];
+            }
+            __syncthreads();
+            staged = bd.index;
+        }
+        const uint64_t first = (tile - bd.tile_begin) * kTile;
+        const uint64_t last = min(bd.size, first + kTile);
+        uint64_t j = first + threadIdx.x;
+        uint64_t next = j < last ? __ldcs(reinterpret_cast<const unsigned long long*>(probes + bd.offset + j)) : 0ull;
+#pragma unroll 1
+        for (; j < last; j += kBatchBlock) {
+            const uint64_t key = next;
+            if (j + kBatchBlock < last)
+                next = __ldcs(reinterpret_cast<const unsigned long long*>(probes + bd.offset + j + kBatchBlock));
+            __stcs(out + bd.offset + j, any_lookup(s_view, s_root, key));
         }
         __syncthreads();
         if (threadIdx.x == 0 && done_ns) {
             __threadfence();
             const unsigned long long done = last - first;
-            const unsigned long long left = atomicAdd(&remaining[b], 0ull - done) - done;
-            if (left == 0) done_ns[b] = globaltimer_ns();
+            const unsigned long long left = atomicAdd(&remaining[s_batch], 0ull - done) - done;
+            if (left == 0) done_ns[s_batch] = globaltimer_ns();
         }
     }
 }
@@ -126,64 +141,203 @@ __global__ void k_fill_remaining(const batch_desc* __restrict__ batches, uint32_
         remaining[b] = batches[b].size;
 }
 
+// tile_batch[t] = batch owning tile t (batches own consecutive tile ranges)
+__global__ void k_fill_tile_map(const batch_desc* __restrict__ batches, uint32_t nb, uint64_t tile_probes,
+                                uint32_t* __restrict__ tile_batch) {
+    for (uint32_t b = blockIdx.x; b < nb; b += gridDim.x) {
+        const uint64_t t0 = batches[b].tile_begin;
+        const uint64_t nt = (batches[b].size + tile_probes - 1) / tile_probes;
+        for (uint64_t t = threadIdx.x; t < nt; t += blockDim.x) tile_batch[t0 + t] = b;
+    }
+}
+
+constexpr uint32_t kTileItems[] = {2, 4, 8, 16};
+
+template <class Fn>
+int with_items(uint32_t items, Fn&& fn) {
+    switch (items) {
+        case 2: return fn(std::integral_constant<int, 2>{});
+        case 4: return fn(std::integral_constant<int, 4>{});
+        case 8: return fn(std::integral_constant<int, 8>{});
+        case 16: return fn(std::integral_constant<int, 16>{});
+        default: set_error("batch plan: tile items must be 2, 4, 8 or 16"); return GJ_ERR_INVALID_ARGUMENT;
+    }
+}
+
 }  // namespace
 }  // namespace gj
 
 using namespace gj;
 
-extern "C" {
+struct gj_batch_plan {
+    int device = 0;
+    std::vector<gj_index*> indexes;
+    std::vector<uint32_t> batch_index;
+    std::vector<uint64_t> offset, size;
+    uint32_t num_batches = 0;
+    uint32_t tile_items = 8;
+    uint64_t tiles = 0;
+    any_view* d_views = nullptr;
+    batch_desc* d_batches = nullptr;
+    uint32_t* d_tile_batch = nullptr;
+    unsigned long long* d_remaining = nullptr;
+    unsigned int* d_counter = nullptr;
+    size_t tile_map_capacity = 0;
+    int grid = 1;
+    // graph cache: the last captured run
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    const void* g_probes = nullptr;
+    const void* g_positions = nullptr;
+    const void* g_done = nullptr;
+    uint32_t g_mode = 0xFFFFFFFFu;
+    uint32_t g_items = 0;
 
-int gj_batch_workspace_size(uint32_t num_indexes, uint32_t num_batches, size_t* bytes) {
-    GJ_CHECK_ARG(bytes, "gj_batch_workspace_size: null argument");
-    *bytes = workspace_carver::need({(size_t)num_indexes * sizeof(any_view), (size_t)num_batches * sizeof(batch_desc),
-                                     (size_t)num_batches * sizeof(unsigned long long), 64});
+    ~gj_batch_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+        cudaFree(d_views);
+        cudaFree(d_batches);
+        cudaFree(d_tile_batch);
+        cudaFree(d_remaining);
+        cudaFree(d_counter);
+    }
+};
+
+namespace {
+
+template <class T>
+int plan_alloc(T** p, size_t count) {
+    GJ_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T)));
     return GJ_OK;
 }
 
-int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32_t* h_batch_index,
-                    const uint64_t* h_probe_offset, const uint64_t* h_batch_size, uint32_t num_batches,
-                    const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode, uint64_t* d_batch_done_ns,
-                    void* d_workspace, size_t workspace_bytes, void* stream) {
-    GJ_CHECK_ARG(indexes && num_indexes > 0, "gj_batch_lookup: no indexes");
-    GJ_CHECK_ARG(num_batches == 0 || (h_batch_index && h_probe_offset && h_batch_size), "gj_batch_lookup: null batch arrays");
-    GJ_CHECK_ARG(mode <= 1, "gj_batch_lookup: mode must be 0 or 1");
-    cudaStream_t s = as_stream(stream);
-    for (uint32_t i = 0; i < num_indexes; ++i) GJ_CHECK_ARG(indexes[i], "gj_batch_lookup: null index");
-    for (uint32_t b = 0; b < num_batches; ++b)
-        GJ_CHECK_ARG(h_batch_index[b] < num_indexes, "gj_batch_lookup: batch refers to a missing index");
-    if (num_batches == 0) return GJ_OK;
-    GJ_CHECK_ARG(d_probes && d_positions, "gj_batch_lookup: null probe or output buffer");
+// descriptors and tile map for the plan's tile shape (synchronous upload)
+int plan_layout(gj_batch_plan* pl, uint32_t items, cudaStream_t s) {
+    const uint64_t tile_probes = (uint64_t)kBatchBlock * items;
+    std::vector<batch_desc> descs(pl->num_batches);
+    uint64_t tiles = 0;
+    for (uint32_t b = 0; b < pl->num_batches; ++b) {
+        descs[b].offset = pl->offset[b];
+        descs[b].size = pl->size[b];
+        descs[b].tile_begin = tiles;
+        descs[b].index = pl->batch_index[b];
+        descs[b].pad = 0;
+        tiles += (pl->size[b] + tile_probes - 1) / tile_probes;
+    }
+    if (tiles > (uint64_t)UINT32_MAX) {
+        set_error("batch plan: too many tiles");
+        return GJ_ERR_TOO_LARGE;
+    }
+    if (tiles > pl->tile_map_capacity) {
+        cudaFree(pl->d_tile_batch);
+        pl->d_tile_batch = nullptr;
+        GJ_TRY(plan_alloc(&pl->d_tile_batch, tiles));
+        pl->tile_map_capacity = tiles;
+    }
+    GJ_CUDA_TRY(cudaMemcpyAsync(pl->d_batches, descs.data(), descs.size() * sizeof(batch_desc), cudaMemcpyHostToDevice,
+                                s));
+    if (pl->num_batches) {
+        k_fill_tile_map<<<pl->num_batches < 4096 ? pl->num_batches : 4096, 256, 0, s>>>(pl->d_batches, pl->num_batches,
+                                                                                      tile_probes, pl->d_tile_batch);
+        GJ_CUDA_TRY(cudaGetLastError());
+    }
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    pl->tiles = tiles;
+    pl->tile_items = items;
+    return with_items(items, [&](auto it) {
+        constexpr int I = decltype(it)::value;
+        device_info di;
+        GJ_TRY(current_device_info(&di));
+        int per_sm = 0;
+        GJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<I>, kBatchBlock, 0));
+        uint64_t grid = (uint64_t)di.sm_count * (per_sm > 0 ? per_sm : 1);
+        if (grid > tiles) grid = tiles ? tiles : 1;
+        pl->grid = (int)grid;
+        return GJ_OK;
+    });
+}
 
+int plan_run(gj_batch_plan* pl, const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode, uint64_t* d_done,
+             cudaStream_t s) {
+    if (pl->num_batches == 0) return GJ_OK;
+    if (d_done) {
+        k_stamp<<<1, 1, 0, s>>>(d_done + pl->num_batches);  // start of the run
+        GJ_CUDA_TRY(cudaGetLastError());
+    }
     if (mode == 1) {
-        for (uint32_t b = 0; b < num_batches; ++b) {
-            GJ_TRY(launch_lookup(indexes[h_batch_index[b]], d_probes + h_probe_offset[b], h_batch_size[b],
-                                 d_positions + h_probe_offset[b], s));
-            if (d_batch_done_ns) k_stamp<<<1, 1, 0, s>>>(d_batch_done_ns + b);
+        for (uint32_t b = 0; b < pl->num_batches; ++b) {
+            GJ_TRY(launch_lookup(pl->indexes[pl->batch_index[b]], d_probes + pl->offset[b], pl->size[b],
+                                 d_positions + pl->offset[b], s));
+            if (d_done) k_stamp<<<1, 1, 0, s>>>(d_done + b);
         }
         GJ_CUDA_TRY(cudaGetLastError());
         return GJ_OK;
     }
-
-    workspace_carver wc(d_workspace, workspace_bytes);
-    any_view* d_views = wc.take<any_view>(num_indexes);
-    batch_desc* d_batches = wc.take<batch_desc>(num_batches);
-    unsigned long long* d_remaining = wc.take<unsigned long long>(num_batches);
-    unsigned int* d_counter = wc.take<unsigned int>(16);
-    if (!d_views || !d_batches || !d_remaining || !d_counter) {
-        set_error("gj_batch_lookup: workspace too small");
-        return GJ_ERR_WORKSPACE;
+    GJ_CUDA_TRY(cudaMemsetAsync(pl->d_counter, 0, sizeof(unsigned int), s));
+    if (d_done) {
+        k_fill_remaining<<<(pl->num_batches + 255) / 256, 256, 0, s>>>(pl->d_batches, pl->num_batches,
+                                                                     pl->d_remaining);
+        GJ_CUDA_TRY(cudaMemsetAsync(d_done, 0, pl->num_batches * sizeof(uint64_t), s));
     }
-    // host staging; pageable uploads return once the driver holds a copy
-    static thread_local std::vector<any_view> views;
-    static thread_local std::vector<batch_desc> descs;
-    views.assign(num_indexes, any_view{});
+    return with_items(pl->tile_items, [&](auto it) {
+        constexpr int I = decltype(it)::value;
+        k_batch<I><<<pl->grid, kBatchBlock, 0, s>>>(pl->d_views, pl->d_batches, pl->d_tile_batch,
+                                                   (uint32_t)pl->tiles, d_probes, d_positions, pl->d_counter,
+                                                   pl->d_remaining, d_done);
+        GJ_CUDA_TRY(cudaGetLastError());
+        return GJ_OK;
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+int gj_batch_plan_create(gj_index* const* indexes, uint32_t num_indexes, const uint32_t* h_batch_index,
+                         const uint64_t* h_probe_offset, const uint64_t* h_batch_size, uint32_t num_batches,
+                         uint32_t tile_items, void* stream, gj_batch_plan** plan) {
+    GJ_CHECK_ARG(plan, "gj_batch_plan_create: null plan");
+    *plan = nullptr;
+    GJ_CHECK_ARG(indexes && num_indexes > 0, "gj_batch_plan_create: no indexes");
+    GJ_CHECK_ARG(num_batches == 0 || (h_batch_index && h_probe_offset && h_batch_size),
+                 "gj_batch_plan_create: null batch arrays");
+    for (uint32_t i = 0; i < num_indexes; ++i) GJ_CHECK_ARG(indexes[i], "gj_batch_plan_create: null index");
+    for (uint32_t b = 0; b < num_batches; ++b)
+        GJ_CHECK_ARG(h_batch_index[b] < num_indexes, "gj_batch_plan_create: batch refers to a missing index");
+    if (tile_items == 0) tile_items = 8;
+    bool ok_items = false;
+    for (uint32_t c : kTileItems) ok_items |= c == tile_items;
+    GJ_CHECK_ARG(ok_items, "gj_batch_plan_create: tile_items must be 2, 4, 8 or 16");
+    cudaStream_t s = as_stream(stream);
+    gj_batch_plan* pl = new (std::nothrow) gj_batch_plan();
+    if (!pl) {
+        set_error("gj_batch_plan_create: out of host memory");
+        return GJ_ERR_OUT_OF_MEMORY;
+    }
+    auto fail = [&](int rc) {
+        delete pl;
+        return rc;
+    };
+    cudaGetDevice(&pl->device);
+    pl->indexes.assign(indexes, indexes + num_indexes);
+    pl->num_batches = num_batches;
+    pl->batch_index.assign(h_batch_index, h_batch_index + num_batches);
+    pl->offset.assign(h_probe_offset, h_probe_offset + num_batches);
+    pl->size.assign(h_batch_size, h_batch_size + num_batches);
+    int rc = plan_alloc(&pl->d_views, num_indexes);
+    if (rc == GJ_OK) rc = plan_alloc(&pl->d_batches, num_batches);
+    if (rc == GJ_OK) rc = plan_alloc(&pl->d_remaining, num_batches);
+    if (rc == GJ_OK) rc = plan_alloc(&pl->d_counter, 4);
+    if (rc != GJ_OK) return fail(rc);
+    std::vector<any_view> views(num_indexes);
     for (uint32_t i = 0; i < num_indexes; ++i) {
         const gj_index* ix = indexes[i];
         any_view& v = views[i];
         std::memset(&v, 0, sizeof(v));
         v.type = ix->type;
         switch (ix->type) {
-            case GJ_INDEX_BINARY_SEARCH: v.u.bs = ix->bs; break;
+            case GJ_INDEX_BINARY_SEARCH: v.u.bs = ix->bs; v.u.bs.fence_slots = 0; break;
             case GJ_INDEX_BTREE: v.u.bt = ix->bt; v.u.bt.cached_levels = 0; break;
             case GJ_INDEX_HARMONIA: v.u.hm = ix->hm; v.u.hm.cached_nodes = 0; v.u.hm.cached_levels = 0; break;
             case GJ_INDEX_RADIX_SPLINE: v.u.rs = ix->rs; break;
@@ -191,35 +345,120 @@ int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32
             default: break;
         }
     }
-    descs.assign(num_batches, batch_desc{});
-    uint64_t tiles = 0;
-    for (uint32_t b = 0; b < num_batches; ++b) {
-        descs[b].offset = h_probe_offset[b];
-        descs[b].size = h_batch_size[b];
-        descs[b].tile_begin = tiles;
-        descs[b].index = h_batch_index[b];
-        tiles += (h_batch_size[b] + kBatchTile - 1) / kBatchTile;
+    if (cudaMemcpyAsync(pl->d_views, views.data(), views.size() * sizeof(any_view), cudaMemcpyHostToDevice, s) !=
+        cudaSuccess) {
+        set_error("gj_batch_plan_create: view upload failed");
+        return fail(GJ_ERR_CUDA);
     }
-    if (tiles > (uint64_t)UINT32_MAX) {
-        set_error("gj_batch_lookup: too many tiles");
-        return GJ_ERR_TOO_LARGE;
+    rc = plan_layout(pl, tile_items, s);
+    if (rc != GJ_OK) return fail(rc);
+    *plan = pl;
+    return GJ_OK;
+}
+
+int gj_batch_plan_free(gj_batch_plan* plan) {
+    delete plan;
+    return GJ_OK;
+}
+
+int gj_batch_plan_tile_items(const gj_batch_plan* plan, uint32_t* tile_items) {
+    GJ_CHECK_ARG(plan && tile_items, "gj_batch_plan_tile_items: null argument");
+    *tile_items = plan->tile_items;
+    return GJ_OK;
+}
+
+int gj_batch_plan_run(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
+                      uint64_t* d_batch_done_ns, void* stream) {
+    GJ_CHECK_ARG(plan, "gj_batch_plan_run: null plan");
+    GJ_CHECK_ARG(mode <= 1, "gj_batch_plan_run: mode must be 0 or 1");
+    GJ_CHECK_ARG(plan->num_batches == 0 || (d_probes && d_positions), "gj_batch_plan_run: null buffer");
+    return plan_run(plan, d_probes, d_positions, mode, d_batch_done_ns, as_stream(stream));
+}
+
+int gj_batch_plan_run_graph(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
+                            uint64_t* d_batch_done_ns, void* stream) {
+    GJ_CHECK_ARG(plan, "gj_batch_plan_run_graph: null plan");
+    GJ_CHECK_ARG(mode <= 1, "gj_batch_plan_run_graph: mode must be 0 or 1");
+    GJ_CHECK_ARG(plan->num_batches == 0 || (d_probes && d_positions), "gj_batch_plan_run_graph: null buffer");
+    cudaStream_t s = as_stream(stream);
+    gj_batch_plan* pl = plan;
+    const bool same = pl->exec && pl->g_probes == d_probes && pl->g_positions == d_positions &&
+                      pl->g_done == d_batch_done_ns && pl->g_mode == mode && pl->g_items == pl->tile_items;
+    if (!same) {
+        if (pl->exec) {
+            cudaGraphExecDestroy(pl->exec);
+            pl->exec = nullptr;
+        }
+        if (!pl->capture_stream) GJ_CUDA_TRY(cudaStreamCreateWithFlags(&pl->capture_stream, cudaStreamNonBlocking));
+        // capture on the plan's own stream: the run enqueues device work only
+        GJ_CUDA_TRY(cudaStreamBeginCapture(pl->capture_stream, cudaStreamCaptureModeRelaxed));
+        const int rc = plan_run(pl, d_probes, d_positions, mode, d_batch_done_ns, pl->capture_stream);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(pl->capture_stream, &graph);
+        if (rc != GJ_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) {
+            set_error("gj_batch_plan_run_graph: capture failed: %s", cudaGetErrorString(e));
+            return GJ_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&pl->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            pl->exec = nullptr;
+            set_error("gj_batch_plan_run_graph: instantiate failed: %s", cudaGetErrorString(ie));
+            return GJ_ERR_CUDA;
+        }
+        pl->g_probes = d_probes;
+        pl->g_positions = d_positions;
+        pl->g_done = d_batch_done_ns;
+        pl->g_mode = mode;
+        pl->g_items = pl->tile_items;
     }
-    GJ_CUDA_TRY(cudaMemcpyAsync(d_views, views.data(), num_indexes * sizeof(any_view), cudaMemcpyHostToDevice, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(d_batches, descs.data(), num_batches * sizeof(batch_desc), cudaMemcpyHostToDevice, s));
-    GJ_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 16 * sizeof(unsigned int), s));
-    if (d_batch_done_ns) {
-        k_fill_remaining<<<(num_batches + 255) / 256, 256, 0, s>>>(d_batches, num_batches, d_remaining);
-        GJ_CUDA_TRY(cudaMemsetAsync(d_batch_done_ns, 0, num_batches * sizeof(uint64_t), s));
+    GJ_CUDA_TRY(cudaGraphLaunch(pl->exec, s));
+    return GJ_OK;
+}
+
+int gj_batch_plan_autotune(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, void* stream,
+                           uint32_t* tile_items, float* best_ms) {
+    GJ_CHECK_ARG(plan, "gj_batch_plan_autotune: null plan");
+    GJ_CHECK_ARG(plan->num_batches == 0 || (d_probes && d_positions), "gj_batch_plan_autotune: null buffer");
+    cudaStream_t s = as_stream(stream);
+    cudaEvent_t a = nullptr, b = nullptr;
+    GJ_CUDA_TRY(cudaEventCreate(&a));
+    GJ_CUDA_TRY(cudaEventCreate(&b));
+    uint32_t best = plan->tile_items;
+    float best_t = -1.f;
+    int rc = GJ_OK;
+    for (uint32_t items : kTileItems) {
+        rc = plan_layout(plan, items, s);
+        if (rc != GJ_OK) break;
+        rc = plan_run(plan, d_probes, d_positions, 0, nullptr, s);  // warm
+        if (rc != GJ_OK) break;
+        cudaEventRecord(a, s);
+        for (int r = 0; r < 3 && rc == GJ_OK; ++r) rc = plan_run(plan, d_probes, d_positions, 0, nullptr, s);
+        cudaEventRecord(b, s);
+        if (rc != GJ_OK || cudaEventSynchronize(b) != cudaSuccess) {
+            if (rc == GJ_OK) {
+                set_error("gj_batch_plan_autotune: timing failed");
+                rc = GJ_ERR_CUDA;
+            }
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (best_t < 0.f || ms < best_t) {
+            best_t = ms;
+            best = items;
+        }
     }
-    device_info di;
-    GJ_TRY(current_device_info(&di));
-    int per_sm = 0;
-    GJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBatchBlock, 0));
-    uint64_t grid = (uint64_t)di.sm_count * (per_sm > 0 ? per_sm : 1);
-    if (grid > tiles) grid = tiles ? tiles : 1;
-    k_batch<<<(unsigned)grid, kBatchBlock, 0, s>>>(d_views, d_batches, num_batches, tiles, d_probes, d_positions,
-                                                   d_counter, d_remaining, d_batch_done_ns);
-    GJ_CUDA_TRY(cudaGetLastError());
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc != GJ_OK) return rc;
+    GJ_TRY(plan_layout(plan, best, s));
+    if (tile_items) *tile_items = best;
+    if (best_ms) *best_ms = best_t / 3.f;
     return GJ_OK;
 }
 

@@ -402,6 +402,12 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
             return GJ_ERR_UNSORTED;
         }
     }
+    if (n > 0 && d_keys) {
+        // key range, kept on the host (partition functions need it per call)
+        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->min_key, d_keys, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->max_key, d_keys + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    }
 
     int rc = GJ_OK;
     switch (type) {

@@ -103,6 +103,7 @@ struct gj_index {
     uint64_t n = 0;
     int device = 0;
     const uint64_t* d_col = nullptr;
+    uint64_t min_key = 0, max_key = 0;  // d_col[0], d_col[n - 1] (0 when empty)
     uint64_t bytes = 0;  // memory_consumption
     gj_index_params params{};
     std::vector<void*> allocations;  // owned device memory

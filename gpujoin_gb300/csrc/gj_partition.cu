@@ -254,17 +254,10 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
     return GJ_OK;
 }
 
-// key range and fanout used by the partitioned INLJ for an index
-int index_key_range(const gj_index* idx, uint64_t* min_key, uint64_t* max_key, cudaStream_t s) {
-    if (idx->n == 0 || !idx->d_col) {
-        *min_key = 0;
-        *max_key = 0;
-        return GJ_OK;
-    }
-    GJ_CUDA_TRY(cudaMemcpyAsync(min_key, idx->d_col, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(max_key, idx->d_col + idx->n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    GJ_CUDA_TRY(cudaStreamSynchronize(s));
-    return GJ_OK;
+// key range used by the partitioned INLJ for an index (recorded at build)
+void index_key_range(const gj_index* idx, uint64_t* min_key, uint64_t* max_key) {
+    *min_key = idx->min_key;
+    *max_key = idx->max_key;
 }
 
 uint32_t default_radix_bits(uint64_t n) {
@@ -370,7 +363,7 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
     if (d_pairs) GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
     if (m == 0) return GJ_OK;
     uint64_t min_key = 0, max_key = 0;
-    GJ_TRY(index_key_range(index, &min_key, &max_key, s));
+    index_key_range(index, &min_key, &max_key);
     const uint32_t shift = shift_for(min_key, max_key, radix_bits);
     for (uint64_t off = 0; off < m; off += w) {
         const uint64_t len = std::min<uint64_t>(w, m - off);

@@ -219,18 +219,55 @@ int gj_learned_mlp_grad(const float* d_params, uint32_t hidden, const float* d_x
                         float* d_grad, double* d_loss, void* stream);
 
 /* ---- batched lookup stream ------------------------------------------------ */
-/* Many probe batches against several indexes (not in the reference).  Batch
- * b probes d_probes[probe_offset[b] .. +batch_size[b]) against
- * indexes[batch_index[b]] and writes d_positions at the same offsets.  The
- * descriptor arrays are host arrays; mode 0 = one persistent kernel over all
- * batches, mode 1 = one launch per batch (the baseline).  If
- * d_batch_done_ns != NULL it receives, per batch, the device globaltimer
- * (ns) when the batch's last probe finished. */
-int gj_batch_lookup(gj_index* const* indexes, uint32_t num_indexes, const uint32_t* h_batch_index,
-                    const uint64_t* h_probe_offset, const uint64_t* h_batch_size, uint32_t num_batches,
-                    const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
-                    uint64_t* d_batch_done_ns, void* d_workspace, size_t workspace_bytes, void* stream);
-int gj_batch_workspace_size(uint32_t num_indexes, uint32_t num_batches, size_t* bytes);
+/* Many probe batches against several indexes (not in the reference, whose
+ * driver runs one index and one probe column per process,
+ * src/index_lookup_new.cu:375-434).  Batch b probes
+ * d_probes[probe_offset[b] .. +batch_size[b]) against indexes[batch_index[b]]
+ * and writes d_positions at the same offsets, with the per-index result
+ * semantics of gj_index_lookup.
+ *
+ * A plan uploads the batch descriptors once (device memory owned by the
+ * plan; the indexes must outlive it).  tile_items (2, 4, 8 or 16; 0 = 8)
+ * sets the persistent kernel's tile: 256 threads x tile_items probes.
+ * Synchronous. */
+typedef struct gj_batch_plan gj_batch_plan;
+int gj_batch_plan_create(gj_index* const* indexes, uint32_t num_indexes, const uint32_t* h_batch_index,
+                         const uint64_t* h_probe_offset, const uint64_t* h_batch_size, uint32_t num_batches,
+                         uint32_t tile_items, void* stream, gj_batch_plan** plan);
+int gj_batch_plan_free(gj_batch_plan* plan);
+int gj_batch_plan_tile_items(const gj_batch_plan* plan, uint32_t* tile_items);
+/* Enqueue a run on the stream: mode 0 = one persistent kernel over all
+ * batches, mode 1 = one lookup launch per batch (the baseline).  Only device
+ * work is enqueued (no host synchronisation, no allocation), so a run can be
+ * captured in a CUDA graph.  If d_batch_done_ns != NULL (num_batches + 1
+ * entries) it receives, per batch, the device globaltimer (ns) when the
+ * batch's last probe finished, and in its last entry the start of the run.
+ * Runs of one plan must not overlap (they share its counters). */
+int gj_batch_plan_run(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
+                      uint64_t* d_batch_done_ns, void* stream);
+/* The same run through a CUDA graph: captured on first use (and again when
+ * the buffers, mode or tile shape change), then replayed with one graph
+ * launch on the stream. */
+int gj_batch_plan_run_graph(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, uint32_t mode,
+                            uint64_t* d_batch_done_ns, void* stream);
+/* Autotuner: time the persistent kernel with every tile shape on these
+ * buffers and keep the fastest in the plan.  Synchronous.  Writes the chosen
+ * tile_items and its time per run (ms) when the pointers are non-null. */
+int gj_batch_plan_autotune(gj_batch_plan* plan, const uint64_t* d_probes, uint32_t* d_positions, void* stream,
+                           uint32_t* tile_items, float* best_ms);
+
+/* ---- autotuners ------------------------------------------------------------ */
+/* Time every candidate on the caller's data (CUDA events on the stream, one
+ * warm-up, best of two) and return the fastest.  They allocate scratch and
+ * synchronise: set-up calls, not part of the probe path.  No counterpart in
+ * the reference, whose experiment_config takes these values as options
+ * (src/index_lookup_config.hpp:18-37).
+ *   partitioned INLJ (pairs): fanout 2^8..2^12 x window {m, m/4, m/16};
+ *   B+tree lookups: node width {4, 8, 16} x leaf width {4, 8, 16, 32}. */
+int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
+                            uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
+int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
+                      uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms);
 
 /* ---- synthetic inputs (src/index_lookup_common.cuh:44-206, src/zipf.hpp) --- */
 /* n strictly increasing keys, iid-uniform in distribution over [0, upper)

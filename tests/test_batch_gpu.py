@@ -40,10 +40,55 @@ def test_batch_modes_match_oracle(orc, gj, cuda):
         exp[a:e] = (orc.exact_lookup if kind in ("btree", "harmonia") else orc.bs_lookup)(col, h_probes[a:e])
     for mode in (0, 1):
         out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
-        done = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        done = torch.zeros(nb + 1, dtype=torch.int64, device="cuda")
         gj.batch_lookup(indexes, which, offs, sizes, probes, out, mode=mode, d_done_ns=done)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(from_dev_u32(out), exp, err_msg=f"mode {mode}")
         d = done.cpu().numpy()
-        nonempty = sizes > 0
-        assert np.all(d[nonempty] > 0), f"mode {mode}: missing completion stamps"
+        nonempty = np.concatenate([sizes > 0, [False]])
+        assert np.all(d[nonempty] >= d[nb]) and d[nb] > 0, f"mode {mode}: missing or early completion stamps"
+
+    # one plan: graph capture and replays, every tile shape, the autotuner
+    plan = gj.batch_plan(indexes, which, offs, sizes, tile_items=2)
+    for items in (2, 4, 8, 16):
+        if items != 2:
+            plan.free()
+            plan = gj.batch_plan(indexes, which, offs, sizes, tile_items=items)
+        assert plan.tile_items == items
+        for rep in range(3):
+            out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+            done = torch.zeros(nb + 1, dtype=torch.int64, device="cuda")
+            plan.run_graph(probes, out, 0, done)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(from_dev_u32(out), exp, err_msg=f"graph items {items} replay {rep}")
+    out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+    best, ms = plan.autotune(probes, out)
+    assert best in (2, 4, 8, 16) and ms > 0 and plan.tile_items == best
+    out.fill_(-7)
+    plan.run_graph(probes, out, 0)
+    plan.run_graph(probes, out, 1)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(from_dev_u32(out), exp, err_msg="after autotune")
+    plan.free()
+
+
+def test_batch_plan_arguments(gj, cuda):
+    import ctypes
+
+    import torch
+
+    keys = torch.arange(0, 4096, dtype=torch.int64, device="cuda") * 3
+    ix = gj.btree_index().construct(None, keys)
+    with pytest.raises(gj.GJError):
+        gj.batch_plan([ix], [1], [0], [10])  # missing index
+    with pytest.raises(gj.GJError):
+        gj.batch_plan([ix], [0], [0], [10], tile_items=3)
+    empty = gj.batch_plan([ix], [], [], [])
+    out = torch.empty(1, dtype=torch.int32, device="cuda")
+    empty.run(keys, out)
+    empty.run_graph(keys, out)
+    torch.cuda.synchronize()
+    empty.free()
+    assert gj.lib().gj_batch_plan_free(None) == 0
+    assert gj.lib().gj_batch_plan_run(None, None, None, 0, None, None) == 1
+    del ctypes

@@ -69,3 +69,14 @@ def test_reference_arm_line(monkeypatch, orc):
     line = json.loads(buf.getvalue().strip())
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_bench_defines_each_function_once():
+    import ast
+    import collections
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py")
+    tree = ast.parse(open(path).read())
+    names = collections.Counter(n.name for n in tree.body if isinstance(n, ast.FunctionDef))
+    assert not [k for k, v in names.items() if v > 1]
