@@ -106,6 +106,8 @@ _SIGNATURES = {
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_status": (_i32, [_vp, _sz, _u64, _vp]),
+    "gj_inlj_pairs_host_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
+    "gj_inlj_pairs_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
@@ -169,6 +171,13 @@ def _stream(stream=None) -> int:
     if stream is None:
         stream = torch.cuda.current_stream()
     return stream.cuda_stream
+
+
+def _hptr(t) -> int:
+    """Address of a contiguous host tensor (pinned memory for the zero-copy entry points)."""
+    if t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous host tensor")
+    return t.data_ptr()
 
 
 def _ptr(t) -> Optional[int]:
@@ -289,6 +298,18 @@ class abstract_index:
         _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
                                    _ptr(workspace), workspace.numel(), _stream(stream)))
         return out_pairs, out_count
+
+    def inlj_pairs_host(self, h_probes, h_pairs, h_count, workspace=None, stream=None):
+        """inlj_pairs on pinned HOST tensors (probes int64, pairs int32 of 2m, count int64 of 1): the
+        kernels read and write host memory directly; the result is valid after the stream syncs."""
+        m = h_probes.numel()
+        if workspace is None:
+            need = _sz(0)
+            _check(lib().gj_inlj_pairs_host_workspace_size(m, ctypes.byref(need)))
+            workspace = _workspace(need.value, _torch().device("cuda", _torch().cuda.current_device()))
+        _check(lib().gj_inlj_pairs_host(self.handle, _hptr(h_probes), m, _hptr(h_pairs), _hptr(h_count),
+                                        _ptr(workspace), workspace.numel(), _stream(stream)))
+        return h_pairs, h_count
 
     @staticmethod
     def inlj_pairs_status(workspace, m: int, stream=None) -> None:

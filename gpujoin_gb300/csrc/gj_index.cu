@@ -528,6 +528,68 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
                         d_pairs ? d_pairs + m : nullptr, as_stream(stream));
 }
 
+// device address of a caller buffer the GPU may touch: pinned or registered
+// host memory (through NVLink-C2C / PCIe), managed or device memory, or
+// pageable host memory on systems where the GPU reads the CPU's page tables
+static int device_address(const void* p, const char* what, void** out) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("%s: not a pointer the CUDA runtime knows", what);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+        if (!a.devicePointer) {
+            set_error("%s: host allocation is not mapped into the device address space", what);
+            return GJ_ERR_INVALID_ARGUMENT;
+        }
+        *out = a.devicePointer;
+        return GJ_OK;
+    }
+    int dev = 0, pageable = 0;
+    GJ_CUDA_TRY(cudaGetDevice(&dev));
+    GJ_CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+    if (!pageable) {
+        set_error("%s: pageable host memory; pin it (cudaHostAlloc / cudaHostRegister)", what);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    *out = const_cast<void*>(p);
+    return GJ_OK;
+}
+
+int gj_inlj_pairs_host_workspace_size(uint64_t m, size_t* bytes) {
+    GJ_CHECK_ARG(bytes, "gj_inlj_pairs_host_workspace_size: null argument");
+    *bytes = pairs_workspace_bytes(m);
+    return GJ_OK;
+}
+
+int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
+                       uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(index && h_count, "gj_inlj_pairs_host: null argument");
+    GJ_CHECK_ARG(m == 0 || (h_probes && h_pairs), "gj_inlj_pairs_host: null buffer");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_inlj_pairs_host: probe rows must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    void *probes = nullptr, *pairs = nullptr, *count = nullptr;
+    GJ_TRY(device_address(h_count, "gj_inlj_pairs_host: count", &count));
+    if (m == 0) {
+        // nothing to launch: the count is written once earlier work on the stream is done
+        GJ_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+        *h_count = 0;
+        return GJ_OK;
+    }
+    GJ_TRY(device_address(h_probes, "gj_inlj_pairs_host: probes", &probes));
+    GJ_TRY(device_address(h_pairs, "gj_inlj_pairs_host: pairs", &pairs));
+    // One pass: each tile reads its probes from host memory, searches them
+    // and writes its pairs back, so host-link reads, searches and writes of
+    // different tiles overlap (a separate compaction pass would serialise
+    // the writes behind the searches).
+    return launch_pairs(index, static_cast<const uint64_t*>(probes), m, nullptr, static_cast<uint32_t*>(pairs),
+                        nullptr, static_cast<uint64_t*>(count), d_workspace, workspace_bytes, nullptr,
+                        as_stream(stream));
+}
+
 int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream) {
     GJ_CHECK_ARG(d_workspace, "gj_inlj_pairs_status: null workspace");
     unsigned int flag = 0;

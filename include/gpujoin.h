@@ -144,6 +144,23 @@ int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* gj_inlj_pairs with the probes, the pairs and the count in HOST memory
+ * (the reference's driver starts from host columns, src/index_lookup_new.cu:
+ * 375-434).  No copies are issued: one kernel reads each tile's probes over
+ * the host link (NVLink-C2C on GB300), searches them and writes the tile's
+ * pairs (and finally *h_count) back, so transfers of some tiles overlap the
+ * searches of others.  The host buffers must be reachable from the GPU:
+ * pinned or registered
+ * (cudaHostAlloc / cudaHostRegister), managed, or pageable on systems whose
+ * GPU uses the CPU's page tables; otherwise GJ_ERR_INVALID_ARGUMENT.
+ * h_pairs holds 2*m uint32; results are valid once the stream has passed
+ * the call (m = 0 waits for the stream and writes *h_count = 0 on the host).
+ * Workspace (device): gj_inlj_pairs_host_workspace_size; gj_inlj_pairs_status
+ * reports a timed-out wait as for gj_inlj_pairs. */
+int gj_inlj_pairs_host_workspace_size(uint64_t m, size_t* bytes);
+int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
+                       uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Outcome of the last gj_inlj_pairs run on this workspace with this m:
  * waits on the stream, then returns GJ_OK or
  * GJ_ERR_TIMEOUT when a bounded device wait of the ordered compaction gave up

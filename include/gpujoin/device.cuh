@@ -47,6 +47,44 @@ GJ_DEVICE_INLINE void ld_sector(const uint64_t* p, uint64_t (&k)[4]) {
         : "l"(p));
 }
 
+// L2 eviction classes for the two kinds of index data: the inner levels of a
+// tree (tens of MB, read by every probe) are kept over the column sectors a
+// probe reads once (hundreds of MB, random).  Loads carry an L2 cache policy;
+// no device-wide setting is involved.
+enum l2_class : int { kL2Default = 0, kL2Keep = 1, kL2Stream = 2 };
+
+template <int kClass>
+GJ_DEVICE_INLINE uint64_t l2_policy() {
+    uint64_t p;
+    if constexpr (kClass == kL2Keep)
+        asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    else
+        asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+template <int kClass>
+GJ_DEVICE_INLINE void ld_sector_c(const uint64_t* p, uint64_t (&k)[4]) {
+    if constexpr (kClass == kL2Default) {
+        ld_sector(p, k);
+    } else {
+        asm("ld.global.nc.L2::cache_hint.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
+            : "=l"(k[0]), "=l"(k[1]), "=l"(k[2]), "=l"(k[3])
+            : "l"(p), "l"(l2_policy<kClass>()));
+    }
+}
+
+template <int kClass>
+GJ_DEVICE_INLINE uint64_t ld_ro_c(const uint64_t* p) {
+    if constexpr (kClass == kL2Default) {
+        return ld_ro(p);
+    } else {
+        uint64_t v;
+        asm("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(l2_policy<kClass>()));
+        return v;
+    }
+}
+
 // branch-free lower bound over any n >= 1 (power-of-two stride form of
 // src/search.cuh:143-158, defined for n == 1 as well)
 GJ_DEVICE_INLINE uint64_t lower_bound_branch_free(const uint64_t* arr, uint64_t n, uint64_t key) {
@@ -76,6 +114,7 @@ GJ_DEVICE_INLINE uint64_t pick4(const uint64_t (&k)[4], uint32_t i) {
 // past it is read with 8-byte loads).  *eq tells whether arr[result] == key
 // (result < hi).  Invariant: in-range keys of sectors below sl are < key,
 // those of sectors above sr are >= key.
+template <int kClass = kL2Default>
 GJ_DEVICE_INLINE uint64_t lower_bound_sectors(const uint64_t* arr, uint64_t arr_n, uint64_t lo, uint64_t hi,
                                               uint64_t key, bool aligned, bool* eq) {
     *eq = false;
@@ -99,10 +138,10 @@ GJ_DEVICE_INLINE uint64_t lower_bound_sectors(const uint64_t* arr, uint64_t arr_
         const uint32_t s0 = s << 2;
         uint64_t k[4];
         if (n32 - s0 >= 4) {
-            ld_sector(arr + s0, k);
+            ld_sector_c<kClass>(arr + s0, k);
         } else {
 #pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) k[i] = (i < n32 - s0) ? ld_ro(arr + s0 + i) : ~0ull;
+            for (uint32_t i = 0; i < 4; ++i) k[i] = (i < n32 - s0) ? ld_ro_c<kClass>(arr + s0 + i) : ~0ull;
         }
         const uint32_t first = s0 > lo32 ? s0 : lo32;
         const uint32_t last = hi32 - s0 > 4 ? s0 + 4 : hi32;
@@ -204,7 +243,7 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
             k[2] = b.x;
             k[3] = b.y;
         } else {
-            ld_sector(node, k);
+            ld_sector_c<kL2Keep>(node, k);
         }
         return (k[0] < key) + (k[1] < key) + (k[2] < key) + (k[3] < key);
     } else {
@@ -215,7 +254,7 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
             return c + ((node[c] < key) ? 1u : 0u);
         }
         bool eq;
-        return (uint32_t)lower_bound_sectors(node, W, 0, W, key, true, &eq);
+        return (uint32_t)lower_bound_sectors<kL2Keep>(node, W, 0, W, key, true, &eq);
     }
 }
 
@@ -234,7 +273,7 @@ GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cach
     const uint64_t base = (uint64_t)j * v.leaf_keys;
     const uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
     bool eq;
-    const uint64_t pos = lower_bound_sectors(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    const uint64_t pos = lower_bound_sectors<kL2Stream>(v.col, v.n, base, end, key, v.col_aligned, &eq);
     return eq ? (uint32_t)pos : kInvalid;
 }
 
@@ -274,16 +313,17 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
             lb = c + ((node[c] < key) ? 1u : 0u);
             child = cache[(uint64_t)v.cached_nodes * K + pos];
         } else {
-            child = ld_ro(v.children + pos);
+            child = ld_ro_c<kL2Keep>(v.children + pos);
             bool eq;
-            lb = (uint32_t)lower_bound_sectors(v.keys + pos * K, K, 0, K, key, true, &eq);
+            lb = (uint32_t)lower_bound_sectors<kL2Keep>(v.keys + pos * K, K, 0, K, key, true, &eq);
         }
         pos = child + lb;
     }
     // leaf level: node pos covers column [32*pos - inner_size, +32)
     const uint64_t leaf_first = (depth > 1) ? (pos * K - v.inner_size) : 0;
     bool eq;
-    const uint64_t p = lower_bound_sectors(v.col, v.n, leaf_first, leaf_first + K, key, v.col_aligned, &eq);
+    const uint64_t p =
+        lower_bound_sectors<kL2Stream>(v.col, v.n, leaf_first, leaf_first + K, key, v.col_aligned, &eq);
     return eq ? (uint32_t)p : kInvalid;
 }
 
@@ -331,7 +371,7 @@ GJ_DEVICE_INLINE double rs_estimate(const rs_view& v, uint64_t key) {
 GJ_DEVICE_INLINE uint64_t window_lower_bound(const uint64_t* col, uint64_t n, uint64_t b, uint64_t e, uint64_t key,
                                              bool aligned) {
     bool eq;
-    uint64_t pos = lower_bound_sectors(col, n, b, e, key, aligned, &eq);
+    uint64_t pos = lower_bound_sectors<kL2Stream>(col, n, b, e, key, aligned, &eq);
     if ((pos == b && b > 0 && ld_ro(col + b - 1) >= key) || (pos == e && e < n && ld_ro(col + e) < key))
         pos = lower_bound_sectors(col, n, 0, n, key, aligned, &eq);
     return pos;
@@ -440,7 +480,7 @@ GJ_DEVICE_INLINE int64_t learned_predict(const learned_leaf& lf, uint64_t key) {
 GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* root, uint64_t key) {
     const uint32_t li = learned_route(v, root, learned_norm(v, key));
     uint64_t w[4];
-    ld_sector(reinterpret_cast<const uint64_t*>(v.leaves + li), w);
+    ld_sector_c<kL2Keep>(reinterpret_cast<const uint64_t*>(v.leaves + li), w);
     learned_leaf lf;
     lf.x0 = w[0];
     lf.base = (uint32_t)w[1];

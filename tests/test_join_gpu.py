@@ -192,3 +192,25 @@ def test_star_join_full_window_and_empty_window(orc, gj, cuda):
         got = gj.star_join_sum(ix, *args, lo, hi).cpu().numpy()
         num, den = orc.star_join(fk, date, price, disc, dim, flag, lo, hi)
         assert (int(got[0]), int(got[1])) == (num, den)
+
+
+@pytest.mark.parametrize("kind", ["btree", "radix_spline", "learned"])
+@pytest.mark.parametrize("m", [0, 1, 4097, 300001])
+def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m):
+    # probes, pairs and count in pinned host memory, read and written by the kernels
+    import torch
+
+    rng = np.random.default_rng(m + 11)
+    col = column(rng, 32 * 3000)
+    pr = probes_for(rng, col, max(m, 1))[:m]
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    h_pr = torch.from_numpy(pr.view(np.int64).copy()).pin_memory()
+    h_pairs = torch.full((2 * max(m, 1),), -1, dtype=torch.int32).pin_memory()
+    h_cnt = torch.full((1,), -1, dtype=torch.int64).pin_memory()
+    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt)
+    torch.cuda.synchronize()
+    c = int(h_cnt[0])
+    got = h_pairs[: 2 * c].numpy().view(np.uint32).reshape(-1, 2)
+    erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
+    np.testing.assert_array_equal(got[:, 0], erows)
+    np.testing.assert_array_equal(got[:, 1], epos)
