@@ -404,9 +404,13 @@ def partitioned_workload(args, world, rank, device, stream):
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
 
-    # fanout and window from the library's autotuner, on the same probes
-    bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
-    tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3)}
+    # fanout and window from the library's autotuner, on the same probes,
+    # unless both are given
+    if args.radix_bits and args.window:
+        bits, window, tune = args.radix_bits, min(args.window, m), None
+    else:
+        bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
+        tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3)}
     need = ctypes.c_size_t()
     gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
     ws = torch.empty(need.value, dtype=torch.uint8, device=device)
@@ -701,6 +705,8 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
     ap.add_argument("--btree-node-keys", type=int, default=0, help="B+tree inner node width (0 = library default)")
     ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
+    ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")
+    ap.add_argument("--window", type=int, default=0, help="partitioned: window size in probes (0 = autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     return ap.parse_args(argv)

@@ -45,35 +45,51 @@ struct stage_desc {
     uint32_t words1;
 };
 
+// Each op searches one probe.  lookup<kScattered> picks the L2 classes:
+// scattered probes (operator()) keep the inner levels and stream the
+// column; the partitioned kernels, whose nearby probes reuse column sectors
+// and touch a slice of the tree, use the default class.
 struct op_bs {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
     bs_view v;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
         return bs_lookup(v, cache, key);
     }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
 template <int W>
 struct op_btree {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
     btree_view v;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
-        return btree_lookup<W>(v, cache, key);
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
+        return btree_lookup<W, kScattered>(v, cache, key);
     }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
 struct op_harmonia {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
     harmonia_view v;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const {
-        return harmonia_lookup(v, cache, key);
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
+        return harmonia_lookup<kScattered>(v, cache, key);
     }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
 struct op_rs {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
     rs_view v;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const { return rs_lookup(v, key); }
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
+        return rs_lookup<kScattered>(v, key);
+    }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
 struct op_noop {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t) const { return kInvalid; }
     __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
 };
 // the root parameters travel inside the op (a kernel argument): the MLP's
@@ -82,9 +98,11 @@ struct op_learned {
     static constexpr int kMinBlocks = GJ_BLOCKS(4);
     learned_view v;
     learned_root_params p;
-    __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t key) const {
-        return learned_lookup(v, p.w, key);
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
+        return learned_lookup<kScattered>(v, p.w, key);
     }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
 
 __device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd) {
@@ -149,7 +167,7 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const
         if (i >= m) break;
         const uint64_t key = next;
         if (k + 1 < kLookupItems) next = load_probe(keys, i + kBlock, m);
-        const uint32_t r = op(cache, key);
+        const uint32_t r = op.template lookup<false>(cache, key);
         out[__ldcs(rows + i)] = r;
     }
 }
@@ -507,7 +525,7 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 
 #pragma unroll 1
         for (int k = 0; k < kSortItems; ++k) {
             const uint32_t j = k * kBlock + threadIdx.x;
-            s_pos[j] = j < tn ? op(cache, s_key[j]) : kInvalid;
+            s_pos[j] = j < tn ? op.template lookup<false>(cache, s_key[j]) : kInvalid;
         }
     };
     auto row_of = [&](int k, uint64_t) { return s_row[k * kBlock + threadIdx.x]; };

@@ -231,7 +231,7 @@ struct btree_view {
 };
 
 // children below a node: the count of separators < key, in [0, W]
-template <int W>
+template <int W, int kInner = kL2Keep>
 GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, bool in_smem) {
     if constexpr (W == 4) {
         uint64_t k[4];
@@ -243,7 +243,7 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
             k[2] = b.x;
             k[3] = b.y;
         } else {
-            ld_sector_c<kL2Keep>(node, k);
+            ld_sector_c<kInner>(node, k);
         }
         return (k[0] < key) + (k[1] < key) + (k[2] < key) + (k[3] < key);
     } else {
@@ -254,12 +254,18 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
             return c + ((node[c] < key) ? 1u : 0u);
         }
         bool eq;
-        return (uint32_t)lower_bound_sectors<kL2Keep>(node, W, 0, W, key, true, &eq);
+        return (uint32_t)lower_bound_sectors<kInner>(node, W, 0, W, key, true, &eq);
     }
 }
 
-template <int W>
+// kScattered: probes arrive in random key order -- the inner levels are
+// kept in L2 over the column sectors, which are streamed.  Partitioned
+// probes (nearby keys in a row) reuse column sectors and touch only a slice
+// of the inner levels: both use the default class then.
+template <int W, bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
+    constexpr int kInner = kScattered ? kL2Keep : kL2Default;
+    constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
     if (key > v.max_key) return kInvalid;
     constexpr uint32_t F = W + 1;
     // node and leaf numbers are below 2^32 (at most one leaf per key)
@@ -268,12 +274,12 @@ GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cach
     const int first_global = h - (int)v.cached_levels;  // levels <= this come from global memory
     int l = h;
     for (; l > first_global; --l) j = j * F + btree_node_search<W>(cache + v.smem_offset[l] + j * W, key, true);
-    for (; l >= 1; --l) j = j * F + btree_node_search<W>(v.level[l] + (uint64_t)j * W, key, false);
+    for (; l >= 1; --l) j = j * F + btree_node_search<W, kInner>(v.level[l] + (uint64_t)j * W, key, false);
     // leaf j: column slice [j*L, min(j*L + L, n))
     const uint64_t base = (uint64_t)j * v.leaf_keys;
     const uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
     bool eq;
-    const uint64_t pos = lower_bound_sectors<kL2Stream>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    const uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
     return eq ? (uint32_t)pos : kInvalid;
 }
 
@@ -298,7 +304,10 @@ struct harmonia_view {
 // Shared cache layout: cached_nodes * 32 keys, then cached_nodes children.
 // A node's child offset does not depend on the search, so it is loaded
 // alongside the node's keys.
+template <bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t* cache, uint64_t key) {
+    constexpr int kInner = kScattered ? kL2Keep : kL2Default;
+    constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
     constexpr uint32_t K = kHarmoniaKeys;
     uint64_t pos = 0;
     const uint32_t depth = v.depth;
@@ -313,9 +322,9 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
             lb = c + ((node[c] < key) ? 1u : 0u);
             child = cache[(uint64_t)v.cached_nodes * K + pos];
         } else {
-            child = ld_ro_c<kL2Keep>(v.children + pos);
+            child = ld_ro_c<kInner>(v.children + pos);
             bool eq;
-            lb = (uint32_t)lower_bound_sectors<kL2Keep>(v.keys + pos * K, K, 0, K, key, true, &eq);
+            lb = (uint32_t)lower_bound_sectors<kInner>(v.keys + pos * K, K, 0, K, key, true, &eq);
         }
         pos = child + lb;
     }
@@ -323,7 +332,7 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
     const uint64_t leaf_first = (depth > 1) ? (pos * K - v.inner_size) : 0;
     bool eq;
     const uint64_t p =
-        lower_bound_sectors<kL2Stream>(v.col, v.n, leaf_first, leaf_first + K, key, v.col_aligned, &eq);
+        lower_bound_sectors<kColumn>(v.col, v.n, leaf_first, leaf_first + K, key, v.col_aligned, &eq);
     return eq ? (uint32_t)p : kInvalid;
 }
 
@@ -368,22 +377,24 @@ GJ_DEVICE_INLINE double rs_estimate(const rs_view& v, uint64_t key) {
 
 // lower bound inside [b, e), widened to the whole column when the window
 // does not bracket it (possible only for keys outside the column)
+template <bool kScattered = true>
 GJ_DEVICE_INLINE uint64_t window_lower_bound(const uint64_t* col, uint64_t n, uint64_t b, uint64_t e, uint64_t key,
                                              bool aligned) {
     bool eq;
-    uint64_t pos = lower_bound_sectors<kL2Stream>(col, n, b, e, key, aligned, &eq);
+    uint64_t pos = lower_bound_sectors<kScattered ? kL2Stream : kL2Default>(col, n, b, e, key, aligned, &eq);
     if ((pos == b && b > 0 && ld_ro(col + b - 1) >= key) || (pos == e && e < n && ld_ro(col + e) < key))
         pos = lower_bound_sectors(col, n, 0, n, key, aligned, &eq);
     return pos;
 }
 
+template <bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t rs_lookup(const rs_view& v, uint64_t key) {
     const double est = rs_estimate(v, key);
     const double err = (double)v.max_error;
     uint64_t b = est < err ? 0 : (uint64_t)(est - err);
     uint64_t e = (est + err + 2 > (double)v.n) ? v.n : (uint64_t)(est + err + 2);
     if (b > e) b = e;
-    const uint64_t pos = window_lower_bound(v.col, v.n, b, e, key, v.col_aligned);
+    const uint64_t pos = window_lower_bound<kScattered>(v.col, v.n, b, e, key, v.col_aligned);
     return pos < v.n ? (uint32_t)pos : kInvalid;
 }
 
@@ -477,10 +488,11 @@ GJ_DEVICE_INLINE int64_t learned_predict(const learned_leaf& lf, uint64_t key) {
     return (int64_t)lf.base + (int64_t)off;
 }
 
+template <bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* root, uint64_t key) {
     const uint32_t li = learned_route(v, root, learned_norm(v, key));
     uint64_t w[4];
-    ld_sector_c<kL2Keep>(reinterpret_cast<const uint64_t*>(v.leaves + li), w);
+    ld_sector_c<kScattered ? kL2Keep : kL2Default>(reinterpret_cast<const uint64_t*>(v.leaves + li), w);
     learned_leaf lf;
     lf.x0 = w[0];
     lf.base = (uint32_t)w[1];
@@ -496,7 +508,7 @@ GJ_DEVICE_INLINE uint32_t learned_lookup(const learned_view& v, const float* roo
     lo = lo < 0 ? 0 : (lo > n ? n : lo);
     hi = hi < 0 ? 0 : (hi > n ? n : hi);
     if (lo > hi) lo = hi;
-    const uint64_t pos = window_lower_bound(v.col, v.n, (uint64_t)lo, (uint64_t)hi, key, v.col_aligned);
+    const uint64_t pos = window_lower_bound<kScattered>(v.col, v.n, (uint64_t)lo, (uint64_t)hi, key, v.col_aligned);
     return pos < v.n ? (uint32_t)pos : kInvalid;
 }
 
