@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch(const any_view* __restric
     constexpr uint64_t kTile = (uint64_t)kBatchBlock * kItems;
     __shared__ uint32_t s_tile, s_batch;
     __shared__ __align__(16) any_view s_view;
-    __shared__ float s_root[kMlpParams];
+    __shared__ __align__(8) float s_root[kMlpParams];
     uint32_t staged = 0xFFFFFFFFu;  // index whose view is in shared memory
     for (;;) {
         if (threadIdx.x == 0) {

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kTrainBlock) k_linear_sums(const float* __rest
 __global__ void k_route(learned_view v, const float* __restrict__ root, uint32_t* __restrict__ leaf_of,
                         unsigned int* __restrict__ first, unsigned int* __restrict__ last,
                         unsigned int* __restrict__ count) {
-    extern __shared__ float s_root[];
+    extern __shared__ __align__(8) float s_root[];
     const int np = v.root_kind == GJ_LEARNED_ROOT_MLP ? kMlpParams : 2;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s_root[i] = root[i];
     __syncthreads();

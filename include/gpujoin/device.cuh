@@ -442,24 +442,44 @@ struct learned_view {
 
 // root parameters carried by value (a kernel argument): the forward pass then
 // reads its weights as constant-bank operands of its FMAs
-struct learned_root_params {
+struct alignas(8) learned_root_params {
     float w[kMlpParams];
 };
 
+// two fused multiply-adds in one instruction (each lane rounds like fmaf)
+GJ_DEVICE_INLINE float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long ra, rb, rc, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rc) : "f"(c.x), "f"(c.y));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+    float2 d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+    return d;
+}
+
+// The lookup's root function.  Layer 2 sums even and odd inputs in two lanes
+// of packed FMAs (out = b2 + even + odd), half the instructions of a scalar
+// chain; the build routes keys with this same function, so the recorded
+// error windows hold for it.  P must be 8-byte aligned.
 GJ_DEVICE_INLINE float mlp32_forward(const float* P, float x) {
     constexpr int H = kMlpWidth;
-    float h1[H];
+    const float2* W1 = reinterpret_cast<const float2*>(P);
+    const float2* b1 = reinterpret_cast<const float2*>(P + H);
+    float2 h1[H / 2];
 #pragma unroll
-    for (int j = 0; j < H; ++j) {
-        const float a = fmaf(P[j], x, P[H + j]);
-        h1[j] = a > 0.f ? a : 0.f;
+    for (int j = 0; j < H / 2; ++j) {
+        const float2 a = fma2(W1[j], make_float2(x, x), b1[j]);
+        h1[j] = make_float2(a.x > 0.f ? a.x : 0.f, a.y > 0.f ? a.y : 0.f);
     }
     float out = P[4 * H + H * H];  // b3
 #pragma unroll
     for (int o = 0; o < H; ++o) {
-        float a = P[2 * H + H * H + o];  // b2[o]
+        const float2* w = reinterpret_cast<const float2*>(P + 2 * H + o * H);
+        float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int j = 0; j < H; ++j) a = fmaf(P[2 * H + o * H + j], h1[j], a);
+        for (int j = 0; j < H / 2; ++j) s = fma2(w[j], h1[j], s);
+        const float a = P[2 * H + H * H + o] + s.x + s.y;  // b2[o] + even + odd
         out = fmaf(P[3 * H + H * H + o], a > 0.f ? a : 0.f, out);
     }
     return out;
