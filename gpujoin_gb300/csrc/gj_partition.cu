@@ -28,8 +28,17 @@ namespace {
 constexpr int kPartBlock = 512;
 constexpr uint32_t kMaxRadixBits = 12;
 constexpr int kHistUnroll = 4;                                    // keys in flight per thread
+// scatter geometry: block size and resident blocks per SM (its register cap)
+#ifndef GJ_SCATTER_BLOCK
+#define GJ_SCATTER_BLOCK 512
+#endif
+#ifndef GJ_SCATTER_PER_SM
+#define GJ_SCATTER_PER_SM 3
+#endif
+constexpr int kScatterBlock = GJ_SCATTER_BLOCK;
+constexpr int kScatterPerSM = GJ_SCATTER_PER_SM;
 constexpr int kScatterItems = 8;                                  // keys per thread per tile
-constexpr uint32_t kScatterTile = kPartBlock * kScatterItems;     // 4096 keys
+constexpr uint32_t kScatterTile = kScatterBlock * kScatterItems;
 
 __device__ __forceinline__ uint32_t part_of(uint64_t key, uint64_t min_key, uint32_t shift, uint32_t fanout) {
     if (key <= min_key) return 0;
@@ -83,11 +92,12 @@ __global__ void k_part_offsets(const uint64_t* __restrict__ incl, uint32_t fanou
         offsets[p] = p == 0 ? 0 : (p == fanout ? m : incl[(uint64_t)p * nblocks - 1]);
 }
 
-// out[p] = sum of in[0..p) over count entries, by the whole block
+// out[p] = sum of in[0..p) over count entries, by the whole block of kB threads
+template <int kB>
 __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t count) {
-    __shared__ uint32_t s_warp[kPartBlock / 32];
+    __shared__ uint32_t s_warp[kB / 32];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t per = (count + kPartBlock - 1) / kPartBlock;
+    const uint32_t per = (count + kB - 1) / kB;
     const uint32_t begin = threadIdx.x * per;
     uint32_t sum = 0;
     for (uint32_t q = 0; q < per; ++q)
@@ -101,7 +111,7 @@ __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        constexpr int kWarps = kPartBlock / 32;
+        constexpr int kWarps = kB / 32;
         const uint32_t v = lane < kWarps ? s_warp[lane] : 0u;
         uint32_t w = v;
 #pragma unroll
@@ -128,9 +138,9 @@ __device__ __forceinline__ void block_exclusive_scan(const uint32_t* in, uint32_
 // with consecutive threads on consecutive addresses: whole sectors instead of
 // one scattered 8-byte store per key.  The order inside a partition follows
 // the block and tile order; inside a tile it is not fixed.
-// 3 resident blocks (42 registers, about 52 KB of shared memory each for
-// fanouts up to 2^8)
-__global__ void __launch_bounds__(kPartBlock, 3) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
+// kScatterPerSM resident blocks (the register cap; about 52 KB of shared
+// memory per 512-thread block for fanouts up to 2^8)
+__global__ void __launch_bounds__(kScatterBlock, kScatterPerSM) k_part_scatter(const uint64_t* __restrict__ keys, uint64_t m,
                                                              uint64_t chunk, uint64_t min_key, uint32_t shift,
                                                              uint32_t fanout, const uint64_t* __restrict__ incl,
                                                              uint64_t row_base, uint64_t* __restrict__ out_keys,
@@ -147,30 +157,30 @@ __global__ void __launch_bounds__(kPartBlock, 3) k_part_scatter(const uint64_t* 
     }
     const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
+    static_assert(kScatterTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
     for (uint64_t t0 = b0; t0 < b1; t0 += kScatterTile) {
         const uint32_t tn = b1 - t0 < kScatterTile ? (uint32_t)(b1 - t0) : kScatterTile;
         for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_cnt[p] = 0;
         __syncthreads();
         uint64_t key[kScatterItems];
         uint32_t slot[kScatterItems];  // partition << 13 | rank inside the tile's partition run
-        static_assert(kScatterTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
 #pragma unroll
         for (int k = 0; k < kScatterItems; ++k) {
-            const uint32_t j = k * kPartBlock + threadIdx.x;
+            const uint32_t j = k * kScatterBlock + threadIdx.x;
             key[k] = j < tn ? __ldcs(k64 + t0 + j) : 0ull;
         }
 #pragma unroll
         for (int k = 0; k < kScatterItems; ++k) {
-            const uint32_t j = k * kPartBlock + threadIdx.x;
+            const uint32_t j = k * kScatterBlock + threadIdx.x;
             const uint32_t p = part_of(key[k], min_key, shift, fanout);
             slot[k] = j < tn ? (p << 13) | atomicAdd(&s_cnt[p], 1u) : 0u;
         }
         __syncthreads();
-        block_exclusive_scan(s_cnt, s_start, fanout);
+        block_exclusive_scan<kScatterBlock>(s_cnt, s_start, fanout);
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kScatterItems; ++k) {
-            const uint32_t j = k * kPartBlock + threadIdx.x;
+            const uint32_t j = k * kScatterBlock + threadIdx.x;
             if (j < tn) {
                 const uint32_t q = s_start[slot[k] >> 13] + (slot[k] & ((1u << 13) - 1));
                 s_keys[q] = key[k];
@@ -178,7 +188,7 @@ __global__ void __launch_bounds__(kPartBlock, 3) k_part_scatter(const uint64_t* 
             }
         }
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < tn; j += kPartBlock) {
+        for (uint32_t j = threadIdx.x; j < tn; j += kScatterBlock) {
             const uint64_t k = s_keys[j];
             const uint32_t p = part_of(k, min_key, shift, fanout);
             const uint64_t d = s_dst[p] + (j - s_start[p]);
@@ -203,7 +213,7 @@ struct partition_plan {
 partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
     partition_plan pl;
     pl.fanout = 1u << radix_bits;
-    uint64_t nb = (uint64_t)sm_count * 3;  // the scatter kernel keeps 3 blocks per SM
+    uint64_t nb = (uint64_t)sm_count * kScatterPerSM;  // the scatter kernel's resident blocks
     const uint64_t min_chunk = 4096;
     if (nb * min_chunk > m) nb = std::max<uint64_t>(1, (m + min_chunk - 1) / min_chunk);
     pl.chunk = (m + nb - 1) / nb;
@@ -248,7 +258,7 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
         k_part_offsets<<<(pl.fanout + 256) / 256, 256, 0, s>>>(hist, pl.fanout, pl.nblocks, m, d_offsets);
         GJ_CUDA_TRY(cudaGetLastError());
     }
-    k_part_scatter<<<pl.nblocks, kPartBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist,
+    k_part_scatter<<<pl.nblocks, kScatterBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist,
                                                                 row_base, d_out_keys, d_out_rows);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
