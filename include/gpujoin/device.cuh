@@ -236,8 +236,16 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
     if constexpr (W == 4) {
         uint64_t k[4];
         if (in_smem) {
-            const ulonglong2 a = reinterpret_cast<const ulonglong2*>(node)[0];
-            const ulonglong2 b = reinterpret_cast<const ulonglong2*>(node)[1];
+            // A 16-byte shared load is served 8 lanes at a time, conflict
+            // free when those lanes hit 8 different 16-byte bank groups.
+            // Node j's halves sit in groups 2j and 2j+1 (mod 8), so loading
+            // the low half first would use even groups only; every second
+            // run of 4 nodes loads its high half first instead, and the
+            // first loads of random nodes spread over all 8 groups.  The
+            // count below does not depend on the order.
+            const uint32_t h = (uint32_t)(reinterpret_cast<uintptr_t>(node) >> 7) & 1u;
+            const ulonglong2 a = reinterpret_cast<const ulonglong2*>(node)[h];
+            const ulonglong2 b = reinterpret_cast<const ulonglong2*>(node)[h ^ 1u];
             k[0] = a.x;
             k[1] = a.y;
             k[2] = b.x;
