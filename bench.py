@@ -400,17 +400,27 @@ def partitioned_workload(args, world, rank, device, stream):
     n, m = 1 << n_log2, 1 << m_log2
     keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
     probes = gj.generate_probes(keys, m, theta=args.theta, seed=args.seed + 1)
-    ix = gj.make_index(args.indexes.split(",")[0]).construct(None, keys)
+    kind = args.indexes.split(",")[0]
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
 
-    # fanout and window from the library's autotuner, on the same probes,
-    # unless both are given
+    # fanout and window (and for a B+tree its node format) from the library's
+    # autotuners, on the same probes, unless given
+    tune = None
+    params = index_params(args, kind)
     if args.radix_bits and args.window:
-        bits, window, tune = args.radix_bits, min(args.window, m), None
+        bits, window = args.radix_bits, min(args.window, m)
+    elif kind == "btree" and not params:
+        w, lk, bits, window, tuned_ms = gj.autotune_partitioned_btree(keys, probes)
+        params = {"btree_node_keys": w, "btree_leaf_keys": lk}
+        tune = {"btree_node_keys": w, "btree_leaf_keys": lk, "radix_bits": bits, "window": window,
+                "ms": round(tuned_ms, 3)}
     else:
+        ix = gj.make_index(kind, **params).construct(None, keys)
         bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
         tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3)}
+        ix.free()
+    ix = gj.make_index(kind, **params).construct(None, keys)
     need = ctypes.c_size_t()
     gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
     ws = torch.empty(need.value, dtype=torch.uint8, device=device)
@@ -443,7 +453,7 @@ def partitioned_workload(args, world, rank, device, stream):
         args, world, "partitioned INLJ probe tuples/s (1 GB300 per rank), % of HBM roofline",
         world * m * args.steps / (ms / 1e3), "probe tuples/s", per_step,
         f"partitioned INLJ: {n} uniform uint64 keys (2^{n_log2}), {m} Zipf({args.theta}) probes (2^{m_log2}), "
-        f"{ix.type_name()}, range partition 2^{bits}, window {window}",
+        f"{ix.type_name()} {params or 'default build'}, range partition 2^{bits}, window {window}",
         {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune": tune,
                          "plain_pairs_ms_per_step": plain_ms,
                          "plain_pairs_tuples_per_s": m / (plain_ms / 1e3)},

@@ -120,6 +120,9 @@ _SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_float)]),
     "gj_autotune_btree": (_i32, [_vp, _u64, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
                                  ctypes.POINTER(ctypes.c_float)]),
+    "gj_autotune_partitioned_btree": (_i32, [_vp, _u64, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
+                                             ctypes.POINTER(_u32), ctypes.POINTER(_u64),
+                                             ctypes.POINTER(ctypes.c_float)]),
     "gj_batch_plan_create": (_i32, [ctypes.POINTER(_vp), _u32, _vp, _vp, _vp, _u32, _u32, _vp, ctypes.POINTER(_vp)]),
     "gj_batch_plan_free": (_i32, [_vp]),
     "gj_batch_plan_tile_items": (_i32, [_vp, ctypes.POINTER(_u32)]),
@@ -495,6 +498,15 @@ def autotune_partitioned(index, d_probes, stream=None):
     _check(lib().gj_autotune_partitioned(index.handle, _ptr(d_probes), d_probes.numel(), _stream(stream),
                                          ctypes.byref(bits), ctypes.byref(window), ctypes.byref(ms)))
     return bits.value, window.value, ms.value
+
+
+def autotune_partitioned_btree(d_keys, d_probes, stream=None):
+    """Fastest (node_keys, leaf_keys, radix_bits, window_size, ms) of a partitioned INLJ over a B+tree."""
+    w, l, bits, window, ms = _u32(0), _u32(0), _u32(0), _u64(0), ctypes.c_float(0)
+    _check(lib().gj_autotune_partitioned_btree(_ptr(d_keys), d_keys.numel(), _ptr(d_probes), d_probes.numel(),
+                                               _stream(stream), ctypes.byref(w), ctypes.byref(l), ctypes.byref(bits),
+                                               ctypes.byref(window), ctypes.byref(ms)))
+    return w.value, l.value, bits.value, window.value, ms.value
 
 
 def autotune_btree(d_keys, d_probes, stream=None):

@@ -111,6 +111,41 @@ int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uin
     return GJ_OK;
 }
 
+int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m,
+                                  void* stream, uint32_t* node_keys, uint32_t* leaf_keys, uint32_t* radix_bits,
+                                  uint64_t* window_size, float* best_ms) {
+    GJ_CHECK_ARG(node_keys && leaf_keys && radix_bits && window_size, "gj_autotune_partitioned_btree: null argument");
+    GJ_CHECK_ARG(n > 0 && d_keys && m > 0 && d_probes, "gj_autotune_partitioned_btree: empty input");
+    // node formats for probes that arrive grouped by key range: the plain
+    // lookup's best (compressed nodes) lengthens each level's dependent chain,
+    // which the partitioned kernel, with fewer warps, hides less well
+    const uint32_t formats[][2] = {{4, 8}, {4, 16}, {kBtreeCompressed, 4}, {kBtreeCompressed, 8}};
+    float best = -1.f;
+    for (const auto& f : formats) {
+        gj_index_params p;
+        gj_index_params_default(&p);
+        p.btree_node_keys = f[0];
+        p.btree_leaf_keys = f[1];
+        gj_index* ix = nullptr;
+        GJ_TRY(gj_index_build(GJ_INDEX_BTREE, d_keys, nullptr, n, &p, stream, &ix));
+        uint32_t bits = 0;
+        uint64_t window = 0;
+        float t = 0.f;
+        const int rc = gj_autotune_partitioned(ix, d_probes, m, stream, &bits, &window, &t);
+        gj_index_free(ix);
+        GJ_TRY(rc);
+        if (best < 0.f || t < best) {
+            best = t;
+            *node_keys = f[0];
+            *leaf_keys = f[1];
+            *radix_bits = bits;
+            *window_size = window;
+        }
+    }
+    if (best_ms) *best_ms = best;
+    return GJ_OK;
+}
+
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms) {
     GJ_CHECK_ARG(node_keys && leaf_keys, "gj_autotune_btree: null argument");
@@ -120,7 +155,7 @@ int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_prob
     GJ_TRY(pos.alloc(m * sizeof(uint32_t)));
     event_pair ev;
     GJ_TRY(ev.init());
-    const uint32_t widths[] = {4, 8, 16};
+    const uint32_t widths[] = {4, 7, 8, 16};
     const uint32_t leaves[] = {4, 8, 16, 32};
     float best = -1.f;
     for (uint32_t w : widths)

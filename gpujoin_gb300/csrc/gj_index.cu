@@ -98,6 +98,39 @@ __global__ void k_gather_btree_level(const uint64_t* __restrict__ col, uint64_t 
     }
 }
 
+// Compressed level l (W = 7): node j's base from its parent's encoding (the
+// rule the lookup applies), its shift from its subtree's largest key, and 7
+// separator deltas (the last key of each child's subtree; 0xFFFFFFFF for a
+// missing child).  span = column keys under one child of a level-l node.
+__global__ void k_encode_btree_c7(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint64_t nodes,
+                                  const uint32_t* __restrict__ parent, const uint64_t* __restrict__ parent_base,
+                                  uint64_t min_key, uint64_t* __restrict__ base_out, uint32_t* __restrict__ out) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nodes; j += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t B = min_key;
+        if (parent) {
+            const uint64_t p = j >> 3, c = j & 7;
+            B = parent_base[p];
+            if (c) B += (uint64_t)parent[p * 8 + c] << (parent[p * 8] & 63u);
+        }
+        base_out[j] = B;
+        const uint64_t end = (j + 1) * 8 * span < n ? (j + 1) * 8 * span : n;
+        const uint64_t range = col[end - 1] - B;
+        const unsigned bits = range ? 64u - (unsigned)__clzll(range) : 0u;
+        const uint32_t sh = bits > 31 ? bits - 31 : 0;
+        uint32_t* w = out + j * 8;
+        w[0] = sh;
+        for (uint32_t i = 0; i < 7; ++i) {
+            const uint64_t first = (j * 8 + i) * span;
+            if (first < n) {
+                const uint64_t last = first + span < n ? first + span : n;
+                w[i + 1] = (uint32_t)((col[last - 1] - B) >> sh);
+            } else {
+                w[i + 1] = kBtreeAbsent;
+            }
+        }
+    }
+}
+
 int device_alloc(gj_index* idx, size_t bytes, void** out) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
@@ -153,13 +186,16 @@ int build_binary_search(gj_index* idx, cudaStream_t s) {
 
 int build_btree(gj_index* idx, cudaStream_t s) {
     const uint32_t W = idx->params.btree_node_keys;
-    const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 8;
-    if (!(W == 4 || W == 8 || W == 16 || W == 32 || W == 64) || L == 0 || L > 4096 || (L & (L - 1)) != 0) {
-        set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 8, 16, 32 or 64 separators, "
-                  "leaves of a power of two up to 4096 keys)", W, L);
+    const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 4;
+    if (!(W == 4 || W == kBtreeCompressed || W == 8 || W == 16 || W == 32 || W == 64) || L == 0 || L > 4096 ||
+        (L & (L - 1)) != 0) {
+        set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 7 (compressed), 8, 16, 32 or 64 "
+                  "separators, leaves of a power of two up to 4096 keys)", W, L);
         return GJ_ERR_INVALID_ARGUMENT;
     }
     const uint64_t n = idx->n;
+    const bool compressed = W == kBtreeCompressed;
+    const uint32_t words = compressed ? 4u : W;  // 64-bit words per node
     const uint64_t F = (uint64_t)W + 1;
     // level sizes: level l has ceil(nodes[l-1] / F) nodes; nodes[0] = leaves
     std::vector<uint64_t> nodes(1, (n + L - 1) / L);
@@ -178,25 +214,61 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     uint64_t total = 0;
     for (uint32_t l = height; l >= 1; --l) {
         offset[l] = total;
-        total += nodes[l] * W;
+        total += nodes[l] * words;
     }
     void* p = nullptr;
     GJ_TRY(device_alloc(idx, total * sizeof(uint64_t), &p));
     uint64_t* base = static_cast<uint64_t*>(p);
-    uint64_t span = L;  // column keys below one child of a level-1 node
-    for (uint32_t l = 1; l <= height; ++l) {
-        const uint64_t slots = nodes[l] * W;
-        const int grid = (int)std::min<uint64_t>((slots + 255) / 256, 65535);
-        k_gather_btree_level<<<grid, 256, 0, s>>>(idx->d_col, n, span, W, slots, base + offset[l]);
-        GJ_CUDA_TRY(cudaGetLastError());
-        idx->bt.level[l] = base + offset[l];
-        span *= F;
+    uint64_t min_key = 0;
+    GJ_CUDA_TRY(cudaMemcpyAsync(&min_key, idx->d_col, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    if (compressed) {
+        // top down: a node's base comes from its parent's encoding
+        uint64_t* bases[2] = {nullptr, nullptr};
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&bases[0]), nodes[1] * sizeof(uint64_t));
+        if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&bases[1]), nodes[1] * sizeof(uint64_t));
+        if (e != cudaSuccess) {
+            cudaFree(bases[0]);
+            set_error("btree: scratch allocation failed: %s", cudaGetErrorString(e));
+            return GJ_ERR_OUT_OF_MEMORY;
+        }
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));  // min_key
+        int rc = GJ_OK;
+        for (uint32_t l = height; l >= 1 && rc == GJ_OK; --l) {
+            const uint64_t span = (uint64_t)L << (3 * (l - 1));
+            const int grid = (int)std::min<uint64_t>((nodes[l] + 255) / 256, 65535);
+            const uint32_t* parent = l == height ? nullptr : reinterpret_cast<const uint32_t*>(base + offset[l + 1]);
+            k_encode_btree_c7<<<grid, 256, 0, s>>>(idx->d_col, n, span, nodes[l], parent, bases[(l + 1) & 1], min_key,
+                                                   bases[l & 1], reinterpret_cast<uint32_t*>(base + offset[l]));
+            if (cudaGetLastError() != cudaSuccess) {
+                set_error("btree: encoding kernel failed to launch");
+                rc = GJ_ERR_CUDA;
+            }
+            idx->bt.level[l] = base + offset[l];
+        }
+        const cudaError_t se = cudaStreamSynchronize(s);
+        cudaFree(bases[0]);
+        cudaFree(bases[1]);
+        GJ_TRY(rc);
+        if (se != cudaSuccess) {
+            set_error("btree: encoding failed: %s", cudaGetErrorString(se));
+            return GJ_ERR_CUDA;
+        }
+    } else {
+        uint64_t span = L;  // column keys below one child of a level-1 node
+        for (uint32_t l = 1; l <= height; ++l) {
+            const uint64_t slots = nodes[l] * W;
+            const int grid = (int)std::min<uint64_t>((slots + 255) / 256, 65535);
+            k_gather_btree_level<<<grid, 256, 0, s>>>(idx->d_col, n, span, W, slots, base + offset[l]);
+            GJ_CUDA_TRY(cudaGetLastError());
+            idx->bt.level[l] = base + offset[l];
+            span *= F;
+        }
     }
     // shared-memory cache: as many top levels as fit the budget
     uint32_t cached = 0;
     uint64_t cache_keys = 0;
     for (uint32_t l = height; l >= 1; --l) {
-        const uint64_t add = nodes[l] * W;
+        const uint64_t add = nodes[l] * words;
         if ((cache_keys + add) * sizeof(uint64_t) > idx->params.smem_cache_bytes) break;
         cache_keys += add;
         cached += 1;
@@ -214,6 +286,7 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     GJ_CUDA_TRY(cudaMemcpyAsync(&maxk, idx->d_col + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     idx->bt.max_key = maxk;
+    idx->bt.min_key = min_key;
     idx->bytes = total * sizeof(uint64_t);
     return GJ_OK;
 }
@@ -311,8 +384,8 @@ void gj_index_params_default(gj_index_params* p) {
     if (!p) return;
     std::memset(p, 0, sizeof(*p));
     p->struct_size = sizeof(gj_index_params);
-    p->btree_node_keys = 4;
-    p->btree_leaf_keys = 8;
+    p->btree_node_keys = kBtreeCompressed;
+    p->btree_leaf_keys = 4;
     p->rs_radix_bits = 18;
     p->rs_max_error = 32;
     p->bs_cache_keys = 4096;

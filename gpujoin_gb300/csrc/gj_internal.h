@@ -152,13 +152,14 @@ size_t scan_workspace_bytes(uint64_t n);
 int inclusive_scan_sum(uint64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
 int inclusive_scan_max_signed(int64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
 
-// B+tree variants compiled: W in {4, 8, 16, 32, 64} separators per node;
-// fn receives std::integral_constant<int, W>
+// B+tree variants compiled: W in {4, 8, 16, 32, 64} separators per node and
+// W = 7 (compressed one-sector nodes); fn receives integral_constant<int, W>
 template <class Fn>
 int btree_dispatch(uint32_t w, Fn&& fn) {
     using std::integral_constant;
     switch (w) {
         case 4: return fn(integral_constant<int, 4>{});
+        case 7: return fn(integral_constant<int, 7>{});
         case 8: return fn(integral_constant<int, 8>{});
         case 16: return fn(integral_constant<int, 16>{});
         case 32: return fn(integral_constant<int, 32>{});

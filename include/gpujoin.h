@@ -65,9 +65,11 @@ typedef enum gj_index_type {
  * (src/indexes.cuh:88-91,169-174,329-334; src/index_lookup_config.hpp:18-37). */
 typedef struct gj_index_params {
     uint32_t struct_size;       /* = sizeof(gj_index_params) */
-    uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout + 1): 4, 8, 16, 32 or 64 (default 4:
-                                   one 32-byte sector per node) */
-    uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 8) */
+    uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout - 1): 4, 8, 16, 32 or 64 uint64
+                                   separators, or 7 (default): one 32-byte sector holding 7 separators as
+                                   32-bit deltas from a base the search carries (fanout 8) */
+    uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 4:
+                                   one 32-byte sector) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */
     uint32_t rs_max_error;      /* RadixSpline spline error (default 32) */
     uint32_t bs_cache_keys;     /* binary search: sampled keys staged in shared memory (default 4096, 0 = off) */
@@ -280,11 +282,17 @@ int gj_batch_plan_autotune(gj_batch_plan* plan, const uint64_t* d_probes, uint32
  * the reference, whose experiment_config takes these values as options
  * (src/index_lookup_config.hpp:18-37).
  *   partitioned INLJ (pairs): fanout 2^8..2^12 x window {m, m/4, m/16};
- *   B+tree lookups: node width {4, 8, 16} x leaf width {4, 8, 16, 32}. */
+ *   B+tree lookups: node width {4, 7 (compressed), 8, 16} x leaf width {4, 8, 16, 32}. */
 int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
                             uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms);
+/* B+tree node format (node x leaf width: 4 x 8, 4 x 16, 7 x 4, 7 x 8) together
+ * with partition fanout and window for the partitioned INLJ of these probes:
+ * gj_autotune_partitioned on a B+tree of each format. */
+int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m,
+                                  void* stream, uint32_t* node_keys, uint32_t* leaf_keys, uint32_t* radix_bits,
+                                  uint64_t* window_size, float* best_ms);
 
 /* ---- synthetic inputs (src/index_lookup_common.cuh:44-206, src/zipf.hpp) --- */
 /* n strictly increasing keys, iid-uniform in distribution over [0, upper)

@@ -219,6 +219,7 @@ GJ_DEVICE_INLINE uint32_t bs_lookup(const bs_view& v, const uint64_t* fence, uin
 struct btree_view {
     const uint64_t* col;
     uint64_t n;
+    uint64_t min_key;                       // col[0]
     uint64_t max_key;                       // col[n-1]
     const uint64_t* level[kBtreeMaxLevels]; // level[l] for l = 1..height (index 0 unused)
     uint32_t smem_offset[kBtreeMaxLevels];  // offset in keys inside the shared cache
@@ -229,6 +230,92 @@ struct btree_view {
     uint32_t leaf_keys;                     // L
     uint32_t col_aligned;                   // column base is 32-byte aligned
 };
+
+// Compressed nodes (W = 7): a node is one 32-byte sector of 8 uint32 words,
+// a header (the node's shift s) and 7 separators stored as deltas
+// d_i = (sep_i - base) >> s, fanout 8.  The base of the root is col[0]; the
+// base of child c of a node (base B, shift s) is B for c = 0 and
+// B + (d_{c-1} << s) otherwise -- never above the child's smallest key.  s is
+// the smallest shift that brings (node max - B) below 2^31, and a missing
+// child's slot holds 0xFFFFFFFF.  With kd = (key - B) >> s, kd > d_i means
+// key > sep_i and kd < d_i means key < sep_i; kd == d_i (same 2^s bucket) is
+// open.
+//
+// The search sends an open slot left (key <= sep_i), which is right for
+// every key equal to a separator -- the common case, probes being column keys
+// -- and needs no extra load.  A wrong left turn (key > sep_i) only ever
+// leads to a leaf whose keys are all below the key, while a correct descent
+// ends in a leaf whose largest key is >= the key; so a leaf search that runs
+// off the leaf's end (before n) reveals it, and only then the search runs
+// again resolving open slots exactly, with the separator (the last key of
+// child i's subtree) read from the column.  kd is clamped below 0xFFFFFFFF
+// for keys that passed a wrong turn.
+constexpr uint32_t kBtreeCompressed = 7;
+constexpr uint32_t kBtreeAbsent = 0xFFFFFFFFu;
+
+GJ_DEVICE_INLINE uint32_t pick8(const uint32_t (&w)[8], uint32_t i) {
+    const uint32_t a = (i & 1) ? w[1] : w[0], b = (i & 1) ? w[3] : w[2];
+    const uint32_t c = (i & 1) ? w[5] : w[4], d = (i & 1) ? w[7] : w[6];
+    const uint32_t lo = (i & 2) ? b : a, hi = (i & 2) ? d : c;
+    return (i & 4) ? hi : lo;
+}
+
+// child of compressed node j (words w, base *B) to descend into; updates *B
+// to the child's base.  span = column keys under one child.
+template <int kInner, bool kExact>
+GJ_DEVICE_INLINE uint32_t btree_c7_child(const btree_view& v, const uint32_t (&w)[8], uint64_t j, uint64_t span,
+                                         uint64_t key, uint64_t* B) {
+    const uint32_t sh = w[0] & 63u;
+    const uint64_t q = (key - *B) >> sh;
+    const uint32_t kd = q < 0xFFFFFFFEull ? (uint32_t)q : 0xFFFFFFFEu;
+    uint32_t c = 0, same = 0;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        c += kd > w[i + 1] ? 1u : 0u;
+        same |= (kd == w[i + 1] ? 1u : 0u) << i;
+    }
+    if constexpr (kExact) {
+        while (same) {  // same 2^s bucket: compare with the exact separator
+            const uint32_t i = __ffs(same) - 1;
+            same &= same - 1;
+            const uint64_t first = (j * 8 + (uint64_t)i) * span;
+            const uint64_t last = first + span < v.n ? first + span : v.n;
+            c += ld_ro_c<kInner>(v.col + last - 1) < key ? 1u : 0u;
+        }
+    }
+    if (c) *B += (uint64_t)pick8(w, c) << sh;
+    return c;
+}
+
+// leaf reached for key through compressed nodes (open slots left, or exact)
+template <int kInner, bool kExact>
+GJ_DEVICE_INLINE uint32_t btree_c7_leaf(const btree_view& v, const uint64_t* cache, uint64_t key) {
+    uint32_t j = 0;
+    uint64_t B = v.min_key;
+    const int h = (int)v.height;
+    const int first_global = h - (int)v.cached_levels;
+    uint64_t span = (uint64_t)v.leaf_keys << (3 * (h - 1));  // column keys under one child at level h
+    int l = h;
+    for (; l > first_global; --l, span >>= 3) {
+        const uint64_t* node = cache + v.smem_offset[l] + (uint64_t)j * 4;
+        // halves in a node-dependent order (bank groups, see btree_node_search)
+        const uint32_t hf = (uint32_t)(reinterpret_cast<uintptr_t>(node) >> 7) & 1u;
+        const ulonglong2 x = reinterpret_cast<const ulonglong2*>(node)[hf];
+        const ulonglong2 y = reinterpret_cast<const ulonglong2*>(node)[hf ^ 1u];
+        const ulonglong2 lo = hf ? y : x, hi = hf ? x : y;
+        const uint32_t w[8] = {(uint32_t)lo.x, (uint32_t)(lo.x >> 32), (uint32_t)lo.y, (uint32_t)(lo.y >> 32),
+                               (uint32_t)hi.x, (uint32_t)(hi.x >> 32), (uint32_t)hi.y, (uint32_t)(hi.y >> 32)};
+        j = j * 8 + btree_c7_child<kInner, kExact>(v, w, j, span, key, &B);
+    }
+    for (; l >= 1; --l, span >>= 3) {
+        uint64_t k[4];
+        ld_sector_c<kInner>(v.level[l] + (uint64_t)j * 4, k);
+        const uint32_t w[8] = {(uint32_t)k[0], (uint32_t)(k[0] >> 32), (uint32_t)k[1], (uint32_t)(k[1] >> 32),
+                               (uint32_t)k[2], (uint32_t)(k[2] >> 32), (uint32_t)k[3], (uint32_t)(k[3] >> 32)};
+        j = j * 8 + btree_c7_child<kInner, kExact>(v, w, j, span, key, &B);
+    }
+    return j;
+}
 
 // children below a node: the count of separators < key, in [0, W]
 template <int W, int kInner = kL2Keep>
@@ -274,6 +361,21 @@ template <int W, bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
     constexpr int kInner = kScattered ? kL2Keep : kL2Default;
     constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
+    if constexpr (W == (int)kBtreeCompressed) {
+        if (key > v.max_key || key < v.min_key) return kInvalid;
+        uint64_t j = btree_c7_leaf<kInner, false>(v, cache, key);
+        uint64_t base = j * v.leaf_keys;
+        uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
+        bool eq;
+        uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+        if (pos == end && end < v.n) {  // a wrong left turn: search again, open slots resolved exactly
+            j = btree_c7_leaf<kInner, true>(v, cache, key);
+            base = j * v.leaf_keys;
+            end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
+            pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+        }
+        return eq ? (uint32_t)pos : kInvalid;
+    }
     if (key > v.max_key) return kInvalid;
     constexpr uint32_t F = W + 1;
     // node and leaf numbers are below 2^32 (at most one leaf per key)

@@ -74,7 +74,8 @@ def test_lookup_small_ragged_sizes(orc, gj, cuda, kind, n):
 
 
 @pytest.mark.parametrize("node_keys,leaf_keys", [(4, 4), (4, 16), (4, 64), (8, 8), (8, 16), (16, 16), (32, 16),
-                                                  (64, 16), (64, 64), (4, 1), (16, 2), (64, 256)])
+                                                  (64, 16), (64, 64), (4, 1), (16, 2), (64, 256), (7, 1), (7, 4),
+                                                  (7, 8), (7, 64)])
 def test_btree_node_widths(orc, gj, cuda, node_keys, leaf_keys):
     import torch
 
@@ -85,6 +86,36 @@ def test_btree_node_widths(orc, gj, cuda, node_keys, leaf_keys):
         ix = gj.btree_index(btree_node_keys=node_keys, btree_leaf_keys=leaf_keys).construct(None, to_dev(torch, col))
         got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
         np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"W={node_keys} L={leaf_keys} n={n}")
+
+
+def compressed_key_sets(rng):
+    top = (1 << 64) - 1
+    dense = np.arange(5, 5 + 70000, dtype=np.uint64)
+    runs = np.concatenate([np.arange(1000, 41000, dtype=np.uint64),
+                           np.arange(1 << 62, (1 << 62) + 30000, dtype=np.uint64) * np.uint64(3),
+                           np.sort(rng.choice(np.arange(1 << 40, (1 << 40) + 200000, dtype=np.uint64), 50000,
+                                              replace=False))])
+    near_top = np.sort(np.uint64(top) - np.arange(0, 90000, dtype=np.uint64) * np.uint64(7))
+    mixed = np.unique(np.concatenate([column(rng, 60000), dense[:20000] * np.uint64(1 << 30)]))
+    return {"dense": dense, "runs": np.unique(runs), "near_top": near_top, "mixed": mixed}
+
+
+@pytest.mark.parametrize("leaf_keys", [1, 8, 64])
+def test_btree_compressed_nodes(orc, gj, cuda, leaf_keys):
+    # one-sector nodes of 32-bit deltas: dense keys (shift 0), runs separated by
+    # huge gaps (large shifts, separators sharing a bucket -> exact comparisons),
+    # keys next to 2^64 - 1, and probes on every key and both neighbours
+    import torch
+
+    rng = np.random.default_rng(leaf_keys + 7)
+    for name, col in compressed_key_sets(rng).items():
+        col = np.ascontiguousarray(col, dtype=np.uint64)
+        pr = np.concatenate([col, col - np.uint64(1), col + np.uint64(1),
+                             rng.integers(0, 1 << 63, 5000, dtype=np.uint64) * np.uint64(2),
+                             np.array([0, 1, (1 << 64) - 1, (1 << 64) - 2, 1 << 63], dtype=np.uint64)])
+        ix = gj.btree_index(btree_node_keys=7, btree_leaf_keys=leaf_keys).construct(None, to_dev(torch, col))
+        got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"{name} L={leaf_keys}")
 
 
 def test_unaligned_column(orc, gj, cuda):
