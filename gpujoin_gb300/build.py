@@ -30,10 +30,17 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+def headers():
+    inc = os.path.join(ROOT, "include")
+    found = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    for d, _, files in os.walk(inc):
+        found += [os.path.join(d, f) for f in files if f.endswith((".h", ".cuh"))]
+    return found
+
+
 def _compile(src: str, extra) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    deps = [src] + [os.path.join(CSRC, "gj_internal.h"), os.path.join(ROOT, "include", "gpujoin.h"),
-                    os.path.join(ROOT, "include", "gpujoin", "device.cuh")]
+    deps = [src] + headers()
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
     cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -50,7 +57,7 @@ def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     extra = shlex.split(os.environ.get("GJ_NVCC_EXTRA", ""))
     srcs = sources()
-    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(os.cpu_count() or 8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]

@@ -67,6 +67,7 @@ __device__ __forceinline__ uint32_t any_lookup(const any_view& v, const float* r
                 case 4: return btree_lookup<4>(v.u.bt, nullptr, key);
                 case 7: return btree_lookup<7>(v.u.bt, nullptr, key);
                 case 8: return btree_lookup<8>(v.u.bt, nullptr, key);
+                case 15: return btree_lookup<15>(v.u.bt, nullptr, key);
                 case 16: return btree_lookup<16>(v.u.bt, nullptr, key);
                 case 32: return btree_lookup<32>(v.u.bt, nullptr, key);
                 default: return btree_lookup<64>(v.u.bt, nullptr, key);

@@ -131,6 +131,39 @@ __global__ void k_encode_btree_c7(const uint64_t* __restrict__ col, uint64_t n, 
     }
 }
 
+// nodes of 16 lanes of 16 bits (node width 15): lane 0 = shift, lanes 1..15 =
+// separators (rounded down) relative to the node's base, at most
+// kBtreeMaxDelta16, kBtreeAbsent16 past the column's end
+__global__ void k_encode_btree_c15(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint64_t nodes,
+                                   const uint16_t* __restrict__ parent, const uint64_t* __restrict__ parent_base,
+                                   uint64_t min_key, uint64_t* __restrict__ base_out, uint16_t* __restrict__ out) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < nodes; j += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t B = min_key;
+        if (parent) {
+            const uint64_t p = j >> 4, c = j & 15;
+            B = parent_base[p];
+            if (c) B += (uint64_t)parent[p * 16 + c] << (parent[p * 16] & 63u);
+        }
+        base_out[j] = B;
+        const uint64_t end = (j + 1) * 16 * span < n ? (j + 1) * 16 * span : n;
+        const uint64_t range = col[end - 1] - B;
+        const unsigned bits = range ? 64u - (unsigned)__clzll(range) : 0u;
+        uint32_t sh = bits > 15 ? bits - 15 : 0;
+        if ((range >> sh) > kBtreeMaxDelta16) sh += 1;
+        uint16_t* w = out + j * 16;
+        w[0] = (uint16_t)sh;
+        for (uint32_t i = 0; i < 15; ++i) {
+            const uint64_t first = (j * 16 + i) * span;
+            if (first < n) {
+                const uint64_t last = first + span < n ? first + span : n;
+                w[i + 1] = (uint16_t)((col[last - 1] - B) >> sh);
+            } else {
+                w[i + 1] = (uint16_t)kBtreeAbsent16;
+            }
+        }
+    }
+}
+
 int device_alloc(gj_index* idx, size_t bytes, void** out) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
@@ -187,14 +220,15 @@ int build_binary_search(gj_index* idx, cudaStream_t s) {
 int build_btree(gj_index* idx, cudaStream_t s) {
     const uint32_t W = idx->params.btree_node_keys;
     const uint32_t L = idx->params.btree_leaf_keys ? idx->params.btree_leaf_keys : 4;
-    if (!(W == 4 || W == kBtreeCompressed || W == 8 || W == 16 || W == 32 || W == 64) || L == 0 || L > 4096 ||
-        (L & (L - 1)) != 0) {
-        set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 7 (compressed), 8, 16, 32 or 64 "
-                  "separators, leaves of a power of two up to 4096 keys)", W, L);
+    if (!(W == 4 || W == kBtreeCompressed || W == 8 || W == kBtreeCompressed16 || W == 16 || W == 32 || W == 64) ||
+        L == 0 || L > 4096 || (L & (L - 1)) != 0) {
+        set_error("btree: node width %u / leaf width %u not supported (nodes of 4, 7 (compressed), 8, 15 "
+                  "(compressed), 16, 32 or 64 separators, leaves of a power of two up to 4096 keys)", W, L);
         return GJ_ERR_INVALID_ARGUMENT;
     }
     const uint64_t n = idx->n;
-    const bool compressed = W == kBtreeCompressed;
+    const bool compressed = W == kBtreeCompressed || W == kBtreeCompressed16;
+    const uint32_t fan_log = W == kBtreeCompressed ? 3u : 4u;  // compressed nodes: log2 of the fanout
     const uint32_t words = compressed ? 4u : W;  // 64-bit words per node
     const uint64_t F = (uint64_t)W + 1;
     // level sizes: level l has ceil(nodes[l-1] / F) nodes; nodes[0] = leaves
@@ -234,11 +268,19 @@ int build_btree(gj_index* idx, cudaStream_t s) {
         GJ_CUDA_TRY(cudaStreamSynchronize(s));  // min_key
         int rc = GJ_OK;
         for (uint32_t l = height; l >= 1 && rc == GJ_OK; --l) {
-            const uint64_t span = (uint64_t)L << (3 * (l - 1));
+            const uint64_t span = (uint64_t)L << (fan_log * (l - 1));
             const int grid = (int)std::min<uint64_t>((nodes[l] + 255) / 256, 65535);
-            const uint32_t* parent = l == height ? nullptr : reinterpret_cast<const uint32_t*>(base + offset[l + 1]);
-            k_encode_btree_c7<<<grid, 256, 0, s>>>(idx->d_col, n, span, nodes[l], parent, bases[(l + 1) & 1], min_key,
-                                                   bases[l & 1], reinterpret_cast<uint32_t*>(base + offset[l]));
+            const uint64_t* parent = l == height ? nullptr : base + offset[l + 1];
+            if (W == kBtreeCompressed)
+                k_encode_btree_c7<<<grid, 256, 0, s>>>(idx->d_col, n, span, nodes[l],
+                                                       reinterpret_cast<const uint32_t*>(parent), bases[(l + 1) & 1],
+                                                       min_key, bases[l & 1],
+                                                       reinterpret_cast<uint32_t*>(base + offset[l]));
+            else
+                k_encode_btree_c15<<<grid, 256, 0, s>>>(idx->d_col, n, span, nodes[l],
+                                                        reinterpret_cast<const uint16_t*>(parent), bases[(l + 1) & 1],
+                                                        min_key, bases[l & 1],
+                                                        reinterpret_cast<uint16_t*>(base + offset[l]));
             if (cudaGetLastError() != cudaSuccess) {
                 set_error("btree: encoding kernel failed to launch");
                 rc = GJ_ERR_CUDA;

@@ -153,7 +153,7 @@ int inclusive_scan_sum(uint64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, 
 int inclusive_scan_max_signed(int64_t* d_data, uint64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
 
 // B+tree variants compiled: W in {4, 8, 16, 32, 64} separators per node and
-// W = 7 (compressed one-sector nodes); fn receives integral_constant<int, W>
+// W = 7, 15 (compressed one-sector nodes); fn receives integral_constant<int, W>
 template <class Fn>
 int btree_dispatch(uint32_t w, Fn&& fn) {
     using std::integral_constant;
@@ -161,6 +161,7 @@ int btree_dispatch(uint32_t w, Fn&& fn) {
         case 4: return fn(integral_constant<int, 4>{});
         case 7: return fn(integral_constant<int, 7>{});
         case 8: return fn(integral_constant<int, 8>{});
+        case 15: return fn(integral_constant<int, 15>{});
         case 16: return fn(integral_constant<int, 16>{});
         case 32: return fn(integral_constant<int, 32>{});
         case 64: return fn(integral_constant<int, 64>{});

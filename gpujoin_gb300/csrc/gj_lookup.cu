@@ -1,709 +1,25 @@
-// gj_lookup.cu -- probe kernels: plain lookup (positions), scattered lookup
-// (partitioned relations) and join-pair materialisation with a deterministic
-// single-pass compaction.
-//
-// Replaces lookup_kernel (src/index_lookup_common.cuh:217-245),
-// partitioned_lookup_kernel (src/index_lookup_partitioning.cu:218-248) and
-// ij_lookup_kernel (src/tpch/tpch_14_ij.cu:371-407).
-//
-// Each kernel is persistent (grid = SMs x resident blocks) and stages the
-// upper part of the index (B+tree top levels, Harmonia top nodes, the sampled
-// binary-search keys) into shared memory once per block.  Probe keys are
-// streamed with evict-first loads, results with streaming stores.
-#include <cuda_runtime.h>
-
-#include <cstdint>
-#include <map>
-#include <mutex>
-#include <utility>
-
-#include "gj_internal.h"
+// gj_lookup.cu -- the library's entry to the probe kernels: dispatch over
+// the index kind to the unit that compiles its kernels, and the kinds
+// compiled here (binary search, no-op).  Kernels: gj_lookup_kernels.cuh.
+#include "gj_lookup_kernels.cuh"
 
 namespace gj {
+
+int lookup_call_bs(const gj_index* idx, const lookup_call& c) { return run_call(op_bs{idx->bs}, idx, c); }
+int lookup_call_noop(const gj_index* idx, const lookup_call& c) { return run_call(op_noop{}, idx, c); }
+
 namespace {
 
-constexpr int kBlock = 256;
-// Resident blocks per SM each lookup kernel is compiled for: the register
-// cap.  A search is a chain of dependent loads and the warps of an SM are
-// what keeps loads in flight, so the tree and search kinds are capped at 32
-// registers (8 blocks of 256 threads, full occupancy), which they meet
-// without spilling; the learned index keeps 64 for its MLP root.
-// GJ_MIN_BLOCKS overrides every kind (tuning builds).
-#ifdef GJ_MIN_BLOCKS
-#define GJ_BLOCKS(n) GJ_MIN_BLOCKS
-#else
-#define GJ_BLOCKS(n) (n)
-#endif
-
-// ---------------------------------------------------------------------------
-// per-index lookup functors
-// ---------------------------------------------------------------------------
-struct stage_desc {
-    const uint64_t* src0;
-    const uint64_t* src1;
-    uint32_t words0;
-    uint32_t words1;
-};
-
-// Each op searches one probe.  lookup<kScattered> picks the L2 classes:
-// scattered probes (operator()) keep the inner levels and stream the
-// column; the partitioned kernels, whose nearby probes reuse column sectors
-// and touch a slice of the tree, use the default class.
-struct op_bs {
-    static constexpr int kMinBlocks = GJ_BLOCKS(8);
-    bs_view v;
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
-        return bs_lookup(v, cache, key);
-    }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
-};
-template <int W>
-struct op_btree {
-    static constexpr int kMinBlocks = GJ_BLOCKS(8);
-    btree_view v;
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
-        return btree_lookup<W, kScattered>(v, cache, key);
-    }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
-};
-struct op_harmonia {
-    static constexpr int kMinBlocks = GJ_BLOCKS(8);
-    harmonia_view v;
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t* cache, uint64_t key) const {
-        return harmonia_lookup<kScattered>(v, cache, key);
-    }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
-};
-struct op_rs {
-    static constexpr int kMinBlocks = GJ_BLOCKS(8);
-    rs_view v;
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
-        return rs_lookup<kScattered>(v, key);
-    }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
-};
-struct op_noop {
-    static constexpr int kMinBlocks = GJ_BLOCKS(8);
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t) const { return kInvalid; }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t*, uint64_t) const { return kInvalid; }
-};
-// the root parameters travel inside the op (a kernel argument): the MLP's
-// FMAs read their weights from the constant bank
-struct op_learned {
-    static constexpr int kMinBlocks = GJ_BLOCKS(4);
-    learned_view v;
-    learned_root_params p;
-    template <bool kScattered = true>
-    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
-        return learned_lookup<kScattered>(v, p.w, key);
-    }
-    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
-};
-
-__device__ __forceinline__ void stage_cache(uint64_t* dst, const stage_desc& sd) {
-    for (uint32_t i = threadIdx.x; i < sd.words0; i += blockDim.x) dst[i] = __ldg(reinterpret_cast<const unsigned long long*>(sd.src0) + i);
-    for (uint32_t i = threadIdx.x; i < sd.words1; i += blockDim.x)
-        dst[sd.words0 + i] = __ldg(reinterpret_cast<const unsigned long long*>(sd.src1) + i);
-    __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// plain lookup: out[i] = lookup(probes[i])
-// ---------------------------------------------------------------------------
-// One block per tile of kLookupItems * kBlock probes (item k of thread t is
-// probe tile + k * kBlock + t: coalesced).  The grid is not persistent: the
-// hardware hands tiles to SMs as they free up, which balances SMs that run
-// at different speeds (near and far HBM of the two dies) without a counter.
-// A thread searches its probes one after another (a search is a chain of
-// dependent loads; occupancy, not per-thread interleaving, keeps many loads
-// in flight) and loads the next probe key before it searches the current
-// one.  No per-thread arrays: the search runs with few live registers.
-#ifndef GJ_LOOKUP_ITEMS
-#define GJ_LOOKUP_ITEMS 8
-#endif
-constexpr int kLookupItems = GJ_LOOKUP_ITEMS;
-constexpr uint32_t kLookupTile = kBlock * kLookupItems;
-
-__device__ __forceinline__ uint64_t load_probe(const uint64_t* p, uint64_t i, uint64_t m) {
-    return i < m ? __ldcs(reinterpret_cast<const unsigned long long*>(p + i)) : 0ull;
-}
-
-template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_lookup(const __grid_constant__ Op op, const stage_desc sd,
-                                                   const uint64_t* __restrict__ probes, uint64_t m,
-                                                   uint32_t* __restrict__ out) {
-    extern __shared__ __align__(16) uint64_t cache[];
-    stage_cache(cache, sd);
-    const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
-    uint64_t next = load_probe(probes, t0, m);
-#pragma unroll 1
-    for (int k = 0; k < kLookupItems; ++k) {
-        const uint64_t i = t0 + (uint64_t)k * kBlock;
-        if (i >= m) break;
-        const uint64_t key = next;
-        if (k + 1 < kLookupItems) next = load_probe(probes, i + kBlock, m);
-        __stcs(out + i, op(cache, key));
-    }
-}
-
-// scattered lookup over a partitioned relation: out[rows[i]] = lookup(keys[i])
-template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const __grid_constant__ Op op, const stage_desc sd,
-                                                           const uint64_t* __restrict__ keys,
-                                                           const uint32_t* __restrict__ rows, uint64_t m,
-                                                           uint32_t* __restrict__ out) {
-    extern __shared__ __align__(16) uint64_t cache[];
-    stage_cache(cache, sd);
-    const uint64_t t0 = (uint64_t)blockIdx.x * kLookupTile + threadIdx.x;
-    uint64_t next = load_probe(keys, t0, m);
-#pragma unroll 1
-    for (int k = 0; k < kLookupItems; ++k) {
-        const uint64_t i = t0 + (uint64_t)k * kBlock;
-        if (i >= m) break;
-        const uint64_t key = next;
-        if (k + 1 < kLookupItems) next = load_probe(keys, i + kBlock, m);
-        const uint32_t r = op.template lookup<false>(cache, key);
-        out[__ldcs(rows + i)] = r;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// join pairs with decoupled look-back compaction
-// ---------------------------------------------------------------------------
-// Pairs are emitted in probe order.  Tiles of kBlock * items probes are
-// claimed in order through an atomic counter, so every predecessor of a tile
-// is already running when the tile looks back: each wait ends.  Waits are
-// bounded anyway; on expiry the kernel raises the error flag (GJ_ERR_TIMEOUT
-// on the host) and stops writing.
-//
-// Plain probes take two passes: k_lookup writes the positions to the upper
-// half of the pairs buffer (the caller provides 2m u32), then
-// k_compact_pairs turns them into pairs.  The search pass has no block
-// barriers, and the compaction is a streaming pass.  Probes of a partitioned
-// relation (row ids, appended behind *d_base) take the single-pass k_pairs.
-constexpr int kItems = GJ_LOOKUP_ITEMS;          // k_pairs items per thread
-constexpr int kCompactItems = 16;                // k_compact_pairs items per thread
-static_assert(kItems >= 4 && (kItems & (kItems - 1)) == 0, "the pairs scan needs a power-of-two item count >= 4");
-constexpr uint32_t kTile = kBlock * kItems;
-// the workspace holds one state per kStateTile probes: enough for the
-// smallest tile of any pairs kernel, at the same offsets for all of them
-constexpr uint32_t kStateTile = kBlock * 4;
-constexpr uint32_t kCompactTile = kBlock * kCompactItems;
-constexpr unsigned long long kFlagAggregate = 1ull << 62;
-constexpr unsigned long long kFlagPrefix = 2ull << 62;
-constexpr unsigned long long kValueMask = (1ull << 62) - 1;
-constexpr uint32_t kSpinLimit = 1u << 22;
-
-struct pairs_ws {
-    unsigned long long* tile_state;  // num_tiles
-    unsigned int* tile_counter;      // 1
-    unsigned int* error;             // 1
-};
-
-// the workspace layout of every pairs kernel; false when it is too small
-inline bool carve_pairs_ws(void* ws, size_t ws_bytes, uint64_t m, pairs_ws* pw, size_t* used) {
-    const uint64_t states = (m + kStateTile - 1) / kStateTile;
-    workspace_carver wc(ws, ws_bytes);
-    pw->tile_state = wc.take<unsigned long long>(states ? states : 1);
-    pw->tile_counter = wc.take<unsigned int>(2);
-    pw->error = pw->tile_counter ? pw->tile_counter + 1 : nullptr;
-    *used = wc.used;
-    return pw->tile_state && pw->tile_counter;
-}
-
-// Exclusive prefix of tile `tile` (> 0) from the states of its predecessors,
-// read 32 at a time by the calling warp: lane i reads tile j - i, and the
-// window is summed up to its nearest published prefix.  Returns false when
-// the wait ran out.
-__device__ __forceinline__ bool look_back(const pairs_ws& ws, uint32_t tile, uint32_t lane,
-                                          unsigned long long* prefix_out) {
-    unsigned long long prefix = 0;
-    int64_t j = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    for (;;) {
-        const int64_t idx = j - (int64_t)lane;
-        const unsigned long long st =
-            idx >= 0 ? *reinterpret_cast<volatile unsigned long long*>(&ws.tile_state[idx]) : (kFlagPrefix | 0ull);
-        const unsigned long long flag = st & ~kValueMask;
-        const uint32_t not_ready = __ballot_sync(0xffffffffu, flag == 0);
-        const uint32_t has_prefix = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-        // lanes up to (and including) the nearest prefix must all be published
-        const uint32_t need = has_prefix ? (2u << (__ffs(has_prefix) - 1)) - 1u : 0xffffffffu;
-        if (not_ready & need) {
-            if (++spins > kSpinLimit) return false;
-            continue;
-        }
-        unsigned long long v = ((need >> lane) & 1u) ? (st & kValueMask) : 0ull;
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-        prefix += v;
-        if (has_prefix) break;
-        j -= 32;
-    }
-    *prefix_out = prefix;
-    return true;
-}
-
-// One block-tile of the ordered compaction: fill(t0, s_pos) writes the
-// result of tile item j into s_pos[j] (kInvalid for no pair) for the tile's
-// kBlock * kIt items; the block then emits the pairs of the tile, in item
-// order, at the tile's prefix.  row_of(k, i) is the probe row of item k of
-// the calling thread (i = t0 + k * kBlock + thread).  Returns false when the
-// kernel must stop (look-back timed out).
-template <int kIt, class Fill, class RowOf>
-__device__ __forceinline__ bool pairs_tile(Fill&& fill, RowOf&& row_of, uint32_t tile, uint2* pairs, uint64_t base,
-                                           uint64_t* __restrict__ d_count, const pairs_ws& ws, uint32_t num_tiles) {
-    constexpr int kWarps = kBlock / 32;
-    constexpr uint32_t kT = kBlock * kIt;
-    __shared__ uint32_t s_cnt[kIt * kWarps];
-    __shared__ uint32_t s_ballot[kIt * kWarps];
-    __shared__ uint32_t s_pos[kT];
-    __shared__ unsigned long long s_prefix;
-    __shared__ int s_abort;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t t0 = (uint64_t)tile * kT;
-    // item k of thread t is probe t0 + k * kBlock + t; output order is probe
-    // order, i.e. (k, warp, lane) order
-    fill(t0, s_pos);
-    uint32_t flags = 0;
-#pragma unroll
-    for (int k = 0; k < kIt; ++k) {
-        const bool hit = s_pos[k * kBlock + threadIdx.x] != kInvalid;
-        const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
-        if (hit) flags |= 1u << k;
-        if (lane == 0) {
-            s_cnt[k * kWarps + warp] = __popc(ballot);
-            s_ballot[k * kWarps + warp] = ballot;
-        }
-    }
-    __syncthreads();
-    if (warp == 0) {
-        // exclusive scan of the kIt * kWarps counts in (k, warp) order
-        constexpr int kPerLane = kIt * kWarps / 32;
-        uint32_t v[kPerLane];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int j = 0; j < kPerLane; ++j) {
-            v[j] = s_cnt[lane * kPerLane + j];
-            sum += v[j];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= (uint32_t)d) incl += t;
-        }
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int j = 0; j < kPerLane; ++j) {
-            s_cnt[lane * kPerLane + j] = run;
-            run += v[j];
-        }
-        // publish the tile aggregate, then resolve the tile prefix
-        const unsigned long long total = __shfl_sync(0xffffffffu, incl, 31);
-        unsigned long long prefix = 0;
-        bool ok = true;
-        if (tile == 0) {
-            if (lane == 0) atomicExch(&ws.tile_state[0], kFlagPrefix | total);
-        } else {
-            if (lane == 0) atomicExch(&ws.tile_state[tile], kFlagAggregate | total);
-            ok = look_back(ws, tile, lane, &prefix);
-            if (lane == 0) {
-                if (ok)
-                    atomicExch(&ws.tile_state[tile], kFlagPrefix | (prefix + total));
-                else
-                    atomicExch(ws.error, 1u);
-            }
-        }
-        if (lane == 0) {
-            s_abort = ok ? 0 : 1;
-            s_prefix = prefix;
-            if (ok && tile == num_tiles - 1) *d_count = base + prefix + total;
-        }
-    }
-    __syncthreads();
-    if (s_abort) return false;
-    const uint64_t tile_base = base + s_prefix;
-#pragma unroll
-    for (int k = 0; k < kIt; ++k) {
-        if (flags & (1u << k)) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            const uint32_t rank = __popc(s_ballot[k * kWarps + warp] & ((1u << lane) - 1u));
-            const uint64_t o = tile_base + s_cnt[k * kWarps + warp] + rank;
-            const uint32_t row = row_of(k, i);
-            const uint32_t pos = s_pos[k * kBlock + threadIdx.x];
-            __stcs(reinterpret_cast<unsigned long long*>(pairs + o), ((unsigned long long)pos << 32) | row);
-        }
-    }
-    __syncthreads();
-    return true;
-}
-
-__device__ __forceinline__ uint32_t claim_tile(const pairs_ws& ws) {
-    __shared__ uint32_t s_tile;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ws.tile_counter, 1u);
-    __syncthreads();
-    return s_tile;
-}
-
-// single pass: search and compact tile by tile (partitioned relations, whose
-// pairs are appended behind *d_base)
-template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const __grid_constant__ Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
-                                                  const uint32_t* __restrict__ rows, uint64_t m,
-                                                  uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
-                                                  uint64_t* __restrict__ d_count, pairs_ws ws, uint32_t num_tiles) {
-    extern __shared__ __align__(16) uint64_t cache[];
-    stage_cache(cache, sd);
-    const uint64_t base = d_base ? *d_base : 0ull;
-    auto search = [&](uint64_t t0, uint32_t* s_pos) {
-        uint64_t next = load_probe(probes, t0 + threadIdx.x, m);
-#pragma unroll 1
-        for (int k = 0; k < kItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            const uint64_t key = next;
-            if (k + 1 < kItems) next = load_probe(probes, i + kBlock, m);
-            s_pos[k * kBlock + threadIdx.x] = i < m ? op(cache, key) : kInvalid;
-        }
-    };
-    for (;;) {
-        const uint32_t tile = claim_tile(ws);
-        if (tile >= num_tiles) break;
-        auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
-        if (!pairs_tile<kItems>(search, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
-    }
-}
-
-// Second pass of the two-pass pairs: compact the positions k_lookup wrote
-// to the stash into pairs at *d_base + (rank of the match).  The stash lies
-// inside the pairs buffer, placed so that the u32 words of pair o only reach
-// stash entries j <= o: a tile writes pairs only after every earlier tile
-// has published its count, i.e. after every earlier tile has read its
-// positions, so no position is overwritten before it is read.  (stash and
-// pairs alias, so neither is __restrict__.)
-__global__ void __launch_bounds__(kBlock) k_compact_pairs(const uint32_t* stash, const uint32_t* __restrict__ rows,
-                                                          uint64_t m, uint2* pairs,
-                                                          const uint64_t* __restrict__ d_base,
-                                                          uint64_t* __restrict__ d_count, pairs_ws ws,
-                                                          uint32_t num_tiles) {
-    const uint64_t base = d_base ? *d_base : 0ull;
-    auto load = [&](uint64_t t0, uint32_t* s_pos) {
-#pragma unroll
-        for (int k = 0; k < kCompactItems; ++k) {
-            const uint64_t i = t0 + (uint64_t)k * kBlock + threadIdx.x;
-            s_pos[k * kBlock + threadIdx.x] = i < m ? __ldcs(stash + i) : kInvalid;
-        }
-    };
-    for (;;) {
-        const uint32_t tile = claim_tile(ws);
-        if (tile >= num_tiles) break;
-        auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
-        if (!pairs_tile<kCompactItems>(load, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
-    }
-}
-
-// Pairs of a partitioned relation (probes grouped by key range, rows
-// attached).  Each tile of kTile probes is first sorted by key in shared
-// memory -- a counting sort over kSortBuckets equal-width buckets of the
-// tile's key range -- and then searched in that order: neighbouring lanes
-// follow the same path through the upper index levels, and a warp-wide load
-// of one sector serves all lanes that ask for it.  Pairs leave in tile order
-// (sorted within a tile, in the relation's order across tiles); the order of
-// equal-bucket keys inside a tile is not fixed.
-constexpr int kSortItems = 4;                        // probes per thread and tile
-constexpr uint32_t kSortTile = kBlock * kSortItems;  // 1024
-constexpr uint32_t kSortBuckets = kSortTile;
-static_assert(kStateTile <= kSortTile && kStateTile <= kTile && kStateTile <= kCompactTile,
-              "the workspace needs a state per tile of every pairs kernel");
-
-__device__ __forceinline__ unsigned bit_length(uint64_t v) { return v ? 64u - (unsigned)__clzll(v) : 0u; }
-
-// about 21 KB of shared memory per block; 6 resident blocks (40 registers),
-// fewer for index kinds compiled for fewer
-template <class Op>
-__global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 6) k_sorted_pairs(const __grid_constant__ Op op, const stage_desc sd,
-                                                         const uint64_t* __restrict__ keys,
-                                                         const uint32_t* __restrict__ rows, uint64_t m,
-                                                         uint2* __restrict__ pairs,
-                                                         const uint64_t* __restrict__ d_base,
-                                                         uint64_t* __restrict__ d_count, pairs_ws ws,
-                                                         uint32_t num_tiles) {
-    extern __shared__ __align__(16) uint64_t cache[];
-    constexpr int kWarps = kBlock / 32;
-    __shared__ uint64_t s_key[kSortTile];
-    __shared__ uint32_t s_row[kSortTile];
-    __shared__ __align__(16) uint32_t s_bucket[kSortBuckets];  // read as uint4
-    __shared__ unsigned long long s_lo[kWarps], s_hi[kWarps];
-    stage_cache(cache, sd);
-    const uint64_t base = d_base ? *d_base : 0ull;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    auto fill = [&](uint64_t t0, uint32_t* s_pos) {
-        const uint32_t tn = m - t0 < kSortTile ? (uint32_t)(m - t0) : kSortTile;
-        uint64_t key[kSortItems];
-        unsigned long long lo = ~0ull, hi = 0ull;
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            key[k] = j < tn ? __ldcs(reinterpret_cast<const unsigned long long*>(keys) + t0 + j) : 0ull;
-            if (j < tn) {
-                lo = key[k] < lo ? key[k] : lo;
-                hi = key[k] > hi ? key[k] : hi;
-            }
-        }
-        // key range of the tile
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) {
-            const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, d);
-            const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, d);
-            lo = a < lo ? a : lo;
-            hi = b > hi ? b : hi;
-        }
-        if (lane == 0) {
-            s_lo[warp] = lo;
-            s_hi[warp] = hi;
-        }
-        for (uint32_t b = threadIdx.x; b < kSortBuckets; b += kBlock) s_bucket[b] = 0;
-        __syncthreads();
-        lo = s_lo[0];
-        hi = s_hi[0];
-#pragma unroll
-        for (int w = 1; w < kWarps; ++w) {
-            lo = s_lo[w] < lo ? s_lo[w] : lo;
-            hi = s_hi[w] > hi ? s_hi[w] : hi;
-        }
-        const unsigned used = bit_length(hi - lo);
-        constexpr unsigned kBucketBits = 10;  // kSortBuckets = 2^10
-        const unsigned sh = used > kBucketBits ? used - kBucketBits : 0;  // (hi - lo) >> sh < kSortBuckets
-        // counting sort: ranks inside a bucket from shared-memory atomics
-        uint32_t rank[kSortItems];
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            rank[k] = j < tn ? atomicAdd(&s_bucket[(uint32_t)((key[k] - lo) >> sh)], 1u) : 0u;
-        }
-        __syncthreads();
-        {
-            // exclusive scan of the buckets: kSortBuckets / kBlock consecutive per thread
-            static_assert(kSortBuckets / kBlock == 4, "one uint4 per thread");
-            uint4* sb = reinterpret_cast<uint4*>(s_bucket) + threadIdx.x;
-            const uint4 c0 = sb[0];
-            const uint32_t sum = c0.x + c0.y + c0.z + c0.w;
-            uint32_t incl = sum;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= (uint32_t)d) incl += t;
-            }
-            __shared__ uint32_t s_wsum[kWarps];
-            if (lane == 31) s_wsum[warp] = incl;
-            __syncthreads();
-            uint32_t run = incl - sum;
-            for (int w = 0; w < (int)warp; ++w) run += s_wsum[w];
-            uint4 o0;
-            o0.x = run; run += c0.x;
-            o0.y = run; run += c0.y;
-            o0.z = run; run += c0.z;
-            o0.w = run;
-            sb[0] = o0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            if (j < tn) {
-                const uint32_t q = s_bucket[(uint32_t)((key[k] - lo) >> sh)] + rank[k];
-                s_key[q] = key[k];
-                s_row[q] = __ldcs(rows + t0 + j);
-            }
-        }
-        __syncthreads();
-#pragma unroll 1
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            s_pos[j] = j < tn ? op.template lookup<false>(cache, s_key[j]) : kInvalid;
-        }
-    };
-    auto row_of = [&](int k, uint64_t) { return s_row[k * kBlock + threadIdx.x]; };
-    for (;;) {
-        const uint32_t tile = claim_tile(ws);
-        if (tile >= num_tiles) break;
-        if (!pairs_tile<kSortItems>(fill, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// dispatch helpers
-// ---------------------------------------------------------------------------
-stage_desc make_stage(const gj_index* idx) {
-    stage_desc sd{};
+int dispatch(const gj_index* idx, const lookup_call& c) {
     switch (idx->type) {
-        case GJ_INDEX_BINARY_SEARCH:
-            if (idx->bs.fence_slots) {
-                sd.src0 = idx->bs.fence;
-                sd.words0 = idx->bs.fence_slots;
-            }
-            break;
+        case GJ_INDEX_BINARY_SEARCH: return lookup_call_bs(idx, c);
         case GJ_INDEX_BTREE:
-            if (idx->bt.cached_levels) {
-                sd.src0 = idx->bt.level[idx->bt.height];
-                sd.words0 = idx->bt.cache_keys;
-            }
-            break;
-        case GJ_INDEX_HARMONIA:
-            if (idx->hm.cached_nodes) {
-                sd.src0 = idx->hm.keys;
-                sd.words0 = idx->hm.cached_nodes * kHarmoniaKeys;
-                sd.src1 = idx->hm.children;
-                sd.words1 = idx->hm.cached_nodes;
-            }
-            break;
-        default:
-            break;
-    }
-    return sd;
-}
-
-size_t stage_bytes(const stage_desc& sd) { return (size_t)(sd.words0 + sd.words1) * sizeof(uint64_t); }
-
-template <class Kernel>
-int prepare_smem(Kernel kernel, size_t smem) {
-    // Static plus dynamic shared memory above 48 KB needs the kernel's
-    // dynamic limit raised first; the limit set so far is remembered per
-    // (device, kernel), so the attribute call is made once per new maximum.
-    if (smem == 0) return GJ_OK;
-    int dev = 0;
-    GJ_CUDA_TRY(cudaGetDevice(&dev));
-    static std::mutex mu;
-    static std::map<std::pair<int, const void*>, size_t> raised;
-    std::lock_guard<std::mutex> lock(mu);
-    size_t& cur = raised[{dev, reinterpret_cast<const void*>(kernel)}];
-    if (smem > cur) {
-        GJ_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        cur = smem;
-    }
-    return GJ_OK;
-}
-
-template <class Kernel>
-int grid_for(Kernel kernel, size_t smem, uint64_t work_items, int* grid) {
-    device_info di;
-    GJ_TRY(current_device_info(&di));
-    GJ_TRY(prepare_smem(kernel, smem));
-    int per_sm = 0;
-    GJ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem));
-    if (per_sm < 1) per_sm = 1;
-    uint64_t g = (uint64_t)di.sm_count * per_sm;
-    const uint64_t need = (work_items + kBlock - 1) / kBlock;
-    if (need < g) g = need ? need : 1;
-    *grid = (int)g;
-    return GJ_OK;
-}
-
-template <class Op>
-int run_lookup(const Op& op, const stage_desc& sd, const uint64_t* probes, uint64_t m, uint32_t* out, cudaStream_t s) {
-    const size_t smem = stage_bytes(sd);
-    GJ_TRY(prepare_smem(k_lookup<Op>, smem));
-    const uint64_t grid = (m + kLookupTile - 1) / kLookupTile;
-    k_lookup<Op><<<(unsigned)grid, kBlock, smem, s>>>(op, sd, probes, m, out);
-    GJ_CUDA_TRY(cudaGetLastError());
-    return GJ_OK;
-}
-
-template <class Op>
-int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const uint32_t* rows, uint64_t m,
-                uint32_t* out, cudaStream_t s) {
-    const size_t smem = stage_bytes(sd);
-    GJ_TRY(prepare_smem(k_scatter_lookup<Op>, smem));
-    const uint64_t grid = (m + kLookupTile - 1) / kLookupTile;
-    k_scatter_lookup<Op><<<(unsigned)grid, kBlock, smem, s>>>(op, sd, keys, rows, m, out);
-    GJ_CUDA_TRY(cudaGetLastError());
-    return GJ_OK;
-}
-
-template <class Op>
-int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const uint32_t* rows, uint64_t m,
-              uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* stash,
-              cudaStream_t s) {
-    const uint32_t num_tiles = (uint32_t)((m + kTile - 1) / kTile);
-    pairs_ws pw;
-    size_t used = 0;
-    if (!carve_pairs_ws(ws, ws_bytes, m, &pw, &used)) {
-        set_error("inlj pairs: workspace of %zu bytes is smaller than the %zu required", ws_bytes,
-                  pairs_workspace_bytes(m));
-        return GJ_ERR_WORKSPACE;
-    }
-    if (m == 0) {
-        if (d_base && d_base != d_count)
-            GJ_CUDA_TRY(cudaMemcpyAsync(d_count, d_base, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
-        else if (!d_base)
-            GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
-        return GJ_OK;
-    }
-    GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
-    if (stash) {
-        GJ_TRY(run_lookup(op, sd, probes, m, stash, s));
-        const uint32_t compact_tiles = (uint32_t)((m + kCompactTile - 1) / kCompactTile);
-        int grid = 0;
-        GJ_TRY(grid_for(k_compact_pairs, 0, (uint64_t)compact_tiles * kBlock, &grid));
-        k_compact_pairs<<<grid, kBlock, 0, s>>>(stash, rows, m, reinterpret_cast<uint2*>(pairs), d_base, d_count, pw,
-                                                compact_tiles);
-        GJ_CUDA_TRY(cudaGetLastError());
-        return GJ_OK;
-    }
-    const size_t smem = stage_bytes(sd);
-    int grid = 0;
-    GJ_TRY(grid_for(k_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));
-    k_pairs<Op><<<grid, kBlock, smem, s>>>(op, sd, probes, rows, m, reinterpret_cast<uint2*>(pairs), d_base, d_count,
-                                           pw, num_tiles);
-    GJ_CUDA_TRY(cudaGetLastError());
-    return GJ_OK;
-}
-
-template <class Op>
-int run_sorted_pairs(const Op& op, const stage_desc& sd, const uint64_t* keys, const uint32_t* rows, uint64_t m,
-                     uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
-                     cudaStream_t s) {
-    const uint32_t num_tiles = (uint32_t)((m + kSortTile - 1) / kSortTile);
-    pairs_ws pw;
-    size_t used = 0;
-    if (!carve_pairs_ws(ws, ws_bytes, m, &pw, &used)) {
-        set_error("partitioned pairs: workspace of %zu bytes is smaller than the %zu required", ws_bytes,
-                  pairs_workspace_bytes(m));
-        return GJ_ERR_WORKSPACE;
-    }
-    if (m == 0) {
-        if (d_base && d_base != d_count)
-            GJ_CUDA_TRY(cudaMemcpyAsync(d_count, d_base, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
-        else if (!d_base)
-            GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
-        return GJ_OK;
-    }
-    GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
-    const size_t smem = stage_bytes(sd);
-    int grid = 0;
-    GJ_TRY(grid_for(k_sorted_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));
-    k_sorted_pairs<Op><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, reinterpret_cast<uint2*>(pairs), d_base,
-                                                  d_count, pw, num_tiles);
-    GJ_CUDA_TRY(cudaGetLastError());
-    return GJ_OK;
-}
-
-// dispatch an action over the index kind
-template <class Fn>
-int with_op(const gj_index* idx, Fn&& fn) {
-    switch (idx->type) {
-        case GJ_INDEX_BINARY_SEARCH: return fn(op_bs{idx->bs});
-        case GJ_INDEX_BTREE:
-            return btree_dispatch(idx->bt.node_keys, [&](auto w) { return fn(op_btree<decltype(w)::value>{idx->bt}); });
-        case GJ_INDEX_HARMONIA: return fn(op_harmonia{idx->hm});
-        case GJ_INDEX_RADIX_SPLINE: return fn(op_rs{idx->rs});
-        case GJ_INDEX_LEARNED: return fn(op_learned{idx->ln, idx->ln_root});
-        case GJ_INDEX_NO_OP: return fn(op_noop{});
+            return btree_dispatch(idx->bt.node_keys,
+                                  [&](auto w) { return lookup_call_btree<decltype(w)::value>(idx, c); });
+        case GJ_INDEX_HARMONIA: return lookup_call_harmonia(idx, c);
+        case GJ_INDEX_RADIX_SPLINE: return lookup_call_rs(idx, c);
+        case GJ_INDEX_LEARNED: return lookup_call_learned(idx, c);
+        case GJ_INDEX_NO_OP: return lookup_call_noop(idx, c);
         default: set_error("unknown index type %d", idx->type); return GJ_ERR_INVALID_ARGUMENT;
     }
 }
@@ -717,33 +33,28 @@ size_t pairs_workspace_bytes(uint64_t m) {
 
 int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s) {
     if (m == 0) return GJ_OK;
-    const stage_desc sd = make_stage(idx);
-    return with_op(idx, [&](const auto& op) { return run_lookup(op, sd, d_probes, m, d_out, s); });
+    return dispatch(idx, {lookup_action::positions, d_probes, nullptr, m, d_out, nullptr, nullptr, nullptr, 0,
+                          nullptr, s});
 }
 
 int launch_scatter_lookup(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
                           uint32_t* d_out, cudaStream_t s) {
     if (m == 0) return GJ_OK;
-    const stage_desc sd = make_stage(idx);
-    return with_op(idx, [&](const auto& op) { return run_scatter(op, sd, d_keys, d_rows, m, d_out, s); });
+    return dispatch(idx, {lookup_action::scatter, d_keys, d_rows, m, d_out, nullptr, nullptr, nullptr, 0, nullptr, s});
 }
 
 int launch_pairs(const gj_index* idx, const uint64_t* d_probes, uint64_t m, const uint32_t* d_rows, uint32_t* d_pairs,
                  const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* d_stash,
                  cudaStream_t s) {
-    const stage_desc sd = make_stage(idx);
-    return with_op(idx, [&](const auto& op) {
-        return run_pairs(op, sd, d_probes, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, d_stash, s);
-    });
+    return dispatch(idx, {lookup_action::pairs, d_probes, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, d_stash,
+                          s});
 }
 
 int launch_partitioned_pairs(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
                              uint32_t* d_pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
                              cudaStream_t s) {
-    const stage_desc sd = make_stage(idx);
-    return with_op(idx, [&](const auto& op) {
-        return run_sorted_pairs(op, sd, d_keys, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes, s);
-    });
+    return dispatch(idx, {lookup_action::sorted_pairs, d_keys, d_rows, m, d_pairs, d_base, d_count, ws, ws_bytes,
+                          nullptr, s});
 }
 
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s) {

@@ -66,8 +66,9 @@ typedef enum gj_index_type {
 typedef struct gj_index_params {
     uint32_t struct_size;       /* = sizeof(gj_index_params) */
     uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout - 1): 4, 8, 16, 32 or 64 uint64
-                                   separators, or 7 (default): one 32-byte sector holding 7 separators as
-                                   32-bit deltas from a base the search carries (fanout 8) */
+                                   separators, or a compressed node of one 32-byte sector holding its
+                                   separators as deltas from a base the search carries: 7 (default; 32-bit
+                                   deltas, fanout 8) or 15 (15-bit deltas, fanout 16) */
     uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 4:
                                    one 32-byte sector) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */
@@ -282,12 +283,12 @@ int gj_batch_plan_autotune(gj_batch_plan* plan, const uint64_t* d_probes, uint32
  * the reference, whose experiment_config takes these values as options
  * (src/index_lookup_config.hpp:18-37).
  *   partitioned INLJ (pairs): fanout 2^8..2^12 x window {m, m/4, m/16};
- *   B+tree lookups: node width {4, 7 (compressed), 8, 16} x leaf width {4, 8, 16, 32}. */
+ *   B+tree lookups: node width {4, 7 (compressed), 8, 15 (compressed), 16} x leaf width {4, 8, 16, 32}. */
 int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
                             uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms);
-/* B+tree node format (node x leaf width: 4 x 8, 4 x 16, 7 x 4, 7 x 8) together
+/* B+tree node format (node x leaf width: 4 x 8, 4 x 16, 7 x 4, 15 x 4) together
  * with partition fanout and window for the partitioned INLJ of these probes:
  * gj_autotune_partitioned on a B+tree of each format. */
 int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m,

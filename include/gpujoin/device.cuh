@@ -287,16 +287,62 @@ GJ_DEVICE_INLINE uint32_t btree_c7_child(const btree_view& v, const uint32_t (&w
     return c;
 }
 
-// leaf reached for key through compressed nodes (open slots left, or exact)
+// Compressed nodes of 16 lanes (node width 15): lane 0 = shift s, lanes
+// 1..15 = separators as (separator - B) >> s, at most kBtreeMaxDelta16;
+// kBtreeAbsent16 past the column's end.  Lane i sits in word i / 2, low half
+// for even i.  Every lane is below 2^15, so one 32-bit subtraction compares
+// two lanes with the probe: (lane | 0x8000) - q keeps bit 15 of its lane iff
+// lane >= q, and no borrow crosses into the other lane.
+constexpr uint32_t kBtreeCompressed16 = 15;
+constexpr uint32_t kBtreeAbsent16 = 0x7FFFu;
+constexpr uint32_t kBtreeMaxDelta16 = 0x7FFEu;
+
+GJ_DEVICE_INLINE uint32_t lane16(const uint32_t (&w)[8], uint32_t i) {
+    const uint32_t x = pick8(w, i >> 1);
+    return (i & 1) ? x >> 16 : x & 0xFFFFu;
+}
+
 template <int kInner, bool kExact>
-GJ_DEVICE_INLINE uint32_t btree_c7_leaf(const btree_view& v, const uint64_t* cache, uint64_t key) {
+GJ_DEVICE_INLINE uint32_t btree_c15_child(const btree_view& v, const uint32_t (&w)[8], uint64_t j, uint64_t span,
+                                          uint64_t key, uint64_t* B) {
+    const uint32_t sh = w[0] & 63u;
+    const uint64_t q = (key - *B) >> sh;
+    const uint32_t kd = q < kBtreeMaxDelta16 ? (uint32_t)q : kBtreeMaxDelta16;
+    const uint32_t q2 = kd * 0x00010001u;
+    uint32_t ge = 0;  // separators >= kd
+#pragma unroll
+    for (int i = 0; i < 8; ++i) ge += __popc(((w[i] | 0x80008000u) - q2) & (i == 0 ? 0x80000000u : 0x80008000u));
+    uint32_t c = 15u - ge;
+    if constexpr (kExact) {
+        // separators equal to kd follow c (they are sorted): step right over
+        // those whose exact key is below the probe
+        for (uint32_t i = c; i < 15u; ++i) {
+            if (lane16(w, i + 1) != kd) break;
+            const uint64_t first = (j * 16 + (uint64_t)i) * span;
+            const uint64_t last = first + span < v.n ? first + span : v.n;
+            if (!(ld_ro_c<kInner>(v.col + last - 1) < key)) break;
+            c = i + 1;
+        }
+    }
+    if (c) *B += (uint64_t)lane16(w, c) << sh;
+    return c;
+}
+
+// leaf reached for key through compressed nodes (open slots left, or exact)
+template <int W, int kInner, bool kExact>
+GJ_DEVICE_INLINE uint32_t btree_cx_leaf(const btree_view& v, const uint64_t* cache, uint64_t key) {
+    constexpr int kLog = W == (int)kBtreeCompressed ? 3 : 4;  // log2 of the fanout
+    auto child = [&](const uint32_t (&w)[8], uint32_t j, uint64_t span, uint64_t* B) {
+        if constexpr (W == (int)kBtreeCompressed) return btree_c7_child<kInner, kExact>(v, w, j, span, key, B);
+        else return btree_c15_child<kInner, kExact>(v, w, j, span, key, B);
+    };
     uint32_t j = 0;
     uint64_t B = v.min_key;
     const int h = (int)v.height;
     const int first_global = h - (int)v.cached_levels;
-    uint64_t span = (uint64_t)v.leaf_keys << (3 * (h - 1));  // column keys under one child at level h
+    uint64_t span = (uint64_t)v.leaf_keys << (kLog * (h - 1));  // column keys under one child at level h
     int l = h;
-    for (; l > first_global; --l, span >>= 3) {
+    for (; l > first_global; --l, span >>= kLog) {
         const uint64_t* node = cache + v.smem_offset[l] + (uint64_t)j * 4;
         // halves in a node-dependent order (bank groups, see btree_node_search)
         const uint32_t hf = (uint32_t)(reinterpret_cast<uintptr_t>(node) >> 7) & 1u;
@@ -305,14 +351,14 @@ GJ_DEVICE_INLINE uint32_t btree_c7_leaf(const btree_view& v, const uint64_t* cac
         const ulonglong2 lo = hf ? y : x, hi = hf ? x : y;
         const uint32_t w[8] = {(uint32_t)lo.x, (uint32_t)(lo.x >> 32), (uint32_t)lo.y, (uint32_t)(lo.y >> 32),
                                (uint32_t)hi.x, (uint32_t)(hi.x >> 32), (uint32_t)hi.y, (uint32_t)(hi.y >> 32)};
-        j = j * 8 + btree_c7_child<kInner, kExact>(v, w, j, span, key, &B);
+        j = (j << kLog) + child(w, j, span, &B);
     }
-    for (; l >= 1; --l, span >>= 3) {
+    for (; l >= 1; --l, span >>= kLog) {
         uint64_t k[4];
         ld_sector_c<kInner>(v.level[l] + (uint64_t)j * 4, k);
         const uint32_t w[8] = {(uint32_t)k[0], (uint32_t)(k[0] >> 32), (uint32_t)k[1], (uint32_t)(k[1] >> 32),
                                (uint32_t)k[2], (uint32_t)(k[2] >> 32), (uint32_t)k[3], (uint32_t)(k[3] >> 32)};
-        j = j * 8 + btree_c7_child<kInner, kExact>(v, w, j, span, key, &B);
+        j = (j << kLog) + child(w, j, span, &B);
     }
     return j;
 }
@@ -361,15 +407,15 @@ template <int W, bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
     constexpr int kInner = kScattered ? kL2Keep : kL2Default;
     constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
-    if constexpr (W == (int)kBtreeCompressed) {
+    if constexpr (W == (int)kBtreeCompressed || W == (int)kBtreeCompressed16) {
         if (key > v.max_key || key < v.min_key) return kInvalid;
-        uint64_t j = btree_c7_leaf<kInner, false>(v, cache, key);
+        uint64_t j = btree_cx_leaf<W, kInner, false>(v, cache, key);
         uint64_t base = j * v.leaf_keys;
         uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
         bool eq;
         uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
         if (pos == end && end < v.n) {  // a wrong left turn: search again, open slots resolved exactly
-            j = btree_c7_leaf<kInner, true>(v, cache, key);
+            j = btree_cx_leaf<W, kInner, true>(v, cache, key);
             base = j * v.leaf_keys;
             end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
             pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
@@ -557,16 +603,7 @@ struct alignas(8) learned_root_params {
 };
 
 // two fused multiply-adds in one instruction (each lane rounds like fmaf)
-GJ_DEVICE_INLINE float2 fma2(float2 a, float2 b, float2 c) {
-    unsigned long long ra, rb, rc, rd;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
-    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
-    asm("mov.b64 %0, {%1, %2};" : "=l"(rc) : "f"(c.x), "f"(c.y));
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
-    float2 d;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
-    return d;
-}
+GJ_DEVICE_INLINE float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // The lookup's root function.  Layer 2 sums even and odd inputs in two lanes
 // of packed FMAs (out = b2 + even + odd), half the instructions of a scalar

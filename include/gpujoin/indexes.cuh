@@ -92,6 +92,7 @@ GJ_DEVICE_INLINE uint32_t btree_lookup_any(const btree_view& v, uint64_t key) {
         case 4: return btree_lookup<4>(v, nullptr, key);
         case 7: return btree_lookup<7>(v, nullptr, key);
         case 8: return btree_lookup<8>(v, nullptr, key);
+        case 15: return btree_lookup<15>(v, nullptr, key);
         case 16: return btree_lookup<16>(v, nullptr, key);
         case 32: return btree_lookup<32>(v, nullptr, key);
         default: return btree_lookup<64>(v, nullptr, key);

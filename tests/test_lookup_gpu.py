@@ -75,7 +75,7 @@ def test_lookup_small_ragged_sizes(orc, gj, cuda, kind, n):
 
 @pytest.mark.parametrize("node_keys,leaf_keys", [(4, 4), (4, 16), (4, 64), (8, 8), (8, 16), (16, 16), (32, 16),
                                                   (64, 16), (64, 64), (4, 1), (16, 2), (64, 256), (7, 1), (7, 4),
-                                                  (7, 8), (7, 64)])
+                                                  (7, 8), (7, 64), (15, 1), (15, 4), (15, 8), (15, 64)])
 def test_btree_node_widths(orc, gj, cuda, node_keys, leaf_keys):
     import torch
 
@@ -100,11 +100,13 @@ def compressed_key_sets(rng):
     return {"dense": dense, "runs": np.unique(runs), "near_top": near_top, "mixed": mixed}
 
 
+@pytest.mark.parametrize("node_keys", [7, 15])
 @pytest.mark.parametrize("leaf_keys", [1, 8, 64])
-def test_btree_compressed_nodes(orc, gj, cuda, leaf_keys):
-    # one-sector nodes of 32-bit deltas: dense keys (shift 0), runs separated by
-    # huge gaps (large shifts, separators sharing a bucket -> exact comparisons),
-    # keys next to 2^64 - 1, and probes on every key and both neighbours
+def test_btree_compressed_nodes(orc, gj, cuda, node_keys, leaf_keys):
+    # one-sector nodes of 32-bit (width 7) or 15-bit (width 15) deltas: dense
+    # keys (shift 0), runs separated by huge gaps (large shifts, separators
+    # sharing a bucket -> exact comparisons), keys next to 2^64 - 1, and probes
+    # on every key and both neighbours
     import torch
 
     rng = np.random.default_rng(leaf_keys + 7)
@@ -113,9 +115,17 @@ def test_btree_compressed_nodes(orc, gj, cuda, leaf_keys):
         pr = np.concatenate([col, col - np.uint64(1), col + np.uint64(1),
                              rng.integers(0, 1 << 63, 5000, dtype=np.uint64) * np.uint64(2),
                              np.array([0, 1, (1 << 64) - 1, (1 << 64) - 2, 1 << 63], dtype=np.uint64)])
-        ix = gj.btree_index(btree_node_keys=7, btree_leaf_keys=leaf_keys).construct(None, to_dev(torch, col))
-        got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
-        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=f"{name} L={leaf_keys}")
+        ix = gj.btree_index(btree_node_keys=node_keys, btree_leaf_keys=leaf_keys).construct(None, to_dev(torch, col))
+        d_pr = to_dev(torch, pr)
+        want = orc.exact_lookup(col, pr)
+        got = from_dev_u32(ix.lookup(d_pr))
+        np.testing.assert_array_equal(got, want, err_msg=f"{name} W={node_keys} L={leaf_keys}")
+        # the partitioned kernels search sorted tiles with the default L2 class
+        got = np.full(len(pr), 0xFFFFFFFF, dtype=np.uint32)
+        _, prs, cnt = ix.partitioned_inlj(d_pr, radix_bits=8, positions=False, pairs=True)
+        p = prs[: 2 * int(cnt.item())].cpu().numpy().view(np.uint32).reshape(-1, 2)
+        got[p[:, 0]] = p[:, 1]
+        np.testing.assert_array_equal(got, want, err_msg=f"partitioned {name} W={node_keys} L={leaf_keys}")
 
 
 def test_unaligned_column(orc, gj, cuda):
