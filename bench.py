@@ -665,7 +665,7 @@ def reference_main(args):
     keys = np.unique(rng.integers(0, 1 << 63, size=n + n // 64, dtype=np.uint64))
     keys = np.sort(rng.choice(keys, size=n, replace=False)) if len(keys) > n else keys
     threads = oracle.hardware_threads()
-    sample = min(args.cpu_sample, m)
+    sample = min(args.ref_sample, m)
     probes = oracle.zipf_probes(keys, sample, args.theta, args.seed + 1, threads)
     tree = oracle.BTree(keys, 247, 246)
     for _ in range(args.warmup):
@@ -712,7 +712,10 @@ def parse_args(argv=None):
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned")
     ap.add_argument("--seed", type=int, default=20261203)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 22)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 28,
+                    help="probes of the CPU baseline leg (one timed pass; about 6 s on 16 Grace cores)")
+    ap.add_argument("--ref-sample", type=int, default=1 << 25,
+                    help="probes per step of --impl reference (all host threads)")
     ap.add_argument("--btree-node-keys", type=int, default=0, help="B+tree inner node width (0 = library default)")
     ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
     ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")

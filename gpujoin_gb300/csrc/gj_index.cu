@@ -426,7 +426,7 @@ void gj_index_params_default(gj_index_params* p) {
     if (!p) return;
     std::memset(p, 0, sizeof(*p));
     p->struct_size = sizeof(gj_index_params);
-    p->btree_node_keys = kBtreeCompressed;
+    p->btree_node_keys = kBtreeCompressed16;
     p->btree_leaf_keys = 4;
     p->rs_radix_bits = 18;
     p->rs_max_error = 32;

@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 
 #include "gj_internal.h"
@@ -94,6 +95,9 @@ struct op_bs {
     }
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };
+// Sorted tiles: an op with a tile_hint searches once per tile for what all
+// keys of the tile's range share (for the B+tree: the deepest node on every
+// path) and starts each probe's search there.
 template <int W>
 struct op_btree {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
@@ -103,6 +107,23 @@ struct op_btree {
         return btree_lookup<W, kScattered>(v, cache, key);
     }
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
+    using tile_hint = btree_cursor;
+    __device__ __forceinline__ tile_hint tile(const uint64_t* cache, uint64_t lo, uint64_t hi) const {
+        return btree_common_node<W, false>(v, cache, lo, hi);
+    }
+    __device__ __forceinline__ uint32_t lookup_in_tile(const uint64_t* cache, uint64_t key, const tile_hint& h) const {
+        return btree_lookup_from<W, false>(v, cache, key, h);
+    }
+};
+
+struct no_tile_hint {};
+template <class Op, class = void>
+struct tile_hint_of {
+    using type = no_tile_hint;
+};
+template <class Op>
+struct tile_hint_of<Op, std::void_t<typename Op::tile_hint>> {
+    using type = typename Op::tile_hint;
 };
 struct op_harmonia {
     static constexpr int kMinBlocks = GJ_BLOCKS(8);
@@ -475,6 +496,9 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 
     __shared__ uint32_t s_row[kSortTile];
     __shared__ __align__(16) uint32_t s_bucket[kSortBuckets];  // read as uint4
     __shared__ unsigned long long s_lo[kWarps], s_hi[kWarps];
+    using hint_t = typename tile_hint_of<Op>::type;
+    constexpr bool kHinted = !std::is_same<hint_t, no_tile_hint>::value;
+    __shared__ hint_t s_hint;
     stage_cache(cache, sd);
     const uint64_t base = d_base ? *d_base : 0ull;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -511,6 +535,9 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 
         for (int w = 1; w < kWarps; ++w) {
             lo = s_lo[w] < lo ? s_lo[w] : lo;
             hi = s_hi[w] > hi ? s_hi[w] : hi;
+        }
+        if constexpr (kHinted) {
+            if (threadIdx.x == 0) s_hint = op.tile(cache, lo, hi);  // read after the barriers below
         }
         const unsigned used = bit_length(hi - lo);
         constexpr unsigned kBucketBits = 10;  // kSortBuckets = 2^10
@@ -558,10 +585,19 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 
             }
         }
         __syncthreads();
+        if constexpr (kHinted) {
+            const hint_t h = s_hint;
 #pragma unroll 1
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            s_pos[j] = j < tn ? op.template lookup<false>(cache, s_key[j]) : kInvalid;
+            for (int k = 0; k < kSortItems; ++k) {
+                const uint32_t j = k * kBlock + threadIdx.x;
+                s_pos[j] = j < tn ? op.lookup_in_tile(cache, s_key[j], h) : kInvalid;
+            }
+        } else {
+#pragma unroll 1
+            for (int k = 0; k < kSortItems; ++k) {
+                const uint32_t j = k * kBlock + threadIdx.x;
+                s_pos[j] = j < tn ? op.template lookup<false>(cache, s_key[j]) : kInvalid;
+            }
         }
     };
     auto row_of = [&](int k, uint64_t) { return s_row[k * kBlock + threadIdx.x]; };

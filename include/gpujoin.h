@@ -67,8 +67,8 @@ typedef struct gj_index_params {
     uint32_t struct_size;       /* = sizeof(gj_index_params) */
     uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout - 1): 4, 8, 16, 32 or 64 uint64
                                    separators, or a compressed node of one 32-byte sector holding its
-                                   separators as deltas from a base the search carries: 7 (default; 32-bit
-                                   deltas, fanout 8) or 15 (15-bit deltas, fanout 16) */
+                                   separators as deltas from a base the search carries: 7 (32-bit deltas,
+                                   fanout 8) or 15 (default; 15-bit deltas, fanout 16) */
     uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 4:
                                    one 32-byte sector) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */

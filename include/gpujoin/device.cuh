@@ -328,37 +328,54 @@ GJ_DEVICE_INLINE uint32_t btree_c15_child(const btree_view& v, const uint32_t (&
     return c;
 }
 
-// leaf reached for key through compressed nodes (open slots left, or exact)
-template <int W, int kInner, bool kExact>
-GJ_DEVICE_INLINE uint32_t btree_cx_leaf(const btree_view& v, const uint64_t* cache, uint64_t key) {
-    constexpr int kLog = W == (int)kBtreeCompressed ? 3 : 4;  // log2 of the fanout
-    auto child = [&](const uint32_t (&w)[8], uint32_t j, uint64_t span, uint64_t* B) {
-        if constexpr (W == (int)kBtreeCompressed) return btree_c7_child<kInner, kExact>(v, w, j, span, key, B);
-        else return btree_c15_child<kInner, kExact>(v, w, j, span, key, B);
-    };
-    uint32_t j = 0;
-    uint64_t B = v.min_key;
-    const int h = (int)v.height;
-    const int first_global = h - (int)v.cached_levels;
-    uint64_t span = (uint64_t)v.leaf_keys << (kLog * (h - 1));  // column keys under one child at level h
-    int l = h;
-    for (; l > first_global; --l, span >>= kLog) {
+// the 8 words of compressed node j of level l, from the shared cache or from
+// global memory
+template <int kInner>
+GJ_DEVICE_INLINE void btree_cx_node(const btree_view& v, const uint64_t* cache, int l, uint32_t j, bool in_smem,
+                                    uint32_t (&w)[8]) {
+    if (in_smem) {
         const uint64_t* node = cache + v.smem_offset[l] + (uint64_t)j * 4;
         // halves in a node-dependent order (bank groups, see btree_node_search)
         const uint32_t hf = (uint32_t)(reinterpret_cast<uintptr_t>(node) >> 7) & 1u;
         const ulonglong2 x = reinterpret_cast<const ulonglong2*>(node)[hf];
         const ulonglong2 y = reinterpret_cast<const ulonglong2*>(node)[hf ^ 1u];
         const ulonglong2 lo = hf ? y : x, hi = hf ? x : y;
-        const uint32_t w[8] = {(uint32_t)lo.x, (uint32_t)(lo.x >> 32), (uint32_t)lo.y, (uint32_t)(lo.y >> 32),
-                               (uint32_t)hi.x, (uint32_t)(hi.x >> 32), (uint32_t)hi.y, (uint32_t)(hi.y >> 32)};
-        j = (j << kLog) + child(w, j, span, &B);
-    }
-    for (; l >= 1; --l, span >>= kLog) {
+        w[0] = (uint32_t)lo.x, w[1] = (uint32_t)(lo.x >> 32), w[2] = (uint32_t)lo.y, w[3] = (uint32_t)(lo.y >> 32);
+        w[4] = (uint32_t)hi.x, w[5] = (uint32_t)(hi.x >> 32), w[6] = (uint32_t)hi.y, w[7] = (uint32_t)(hi.y >> 32);
+    } else {
         uint64_t k[4];
         ld_sector_c<kInner>(v.level[l] + (uint64_t)j * 4, k);
-        const uint32_t w[8] = {(uint32_t)k[0], (uint32_t)(k[0] >> 32), (uint32_t)k[1], (uint32_t)(k[1] >> 32),
-                               (uint32_t)k[2], (uint32_t)(k[2] >> 32), (uint32_t)k[3], (uint32_t)(k[3] >> 32)};
-        j = (j << kLog) + child(w, j, span, &B);
+        w[0] = (uint32_t)k[0], w[1] = (uint32_t)(k[0] >> 32), w[2] = (uint32_t)k[1], w[3] = (uint32_t)(k[1] >> 32);
+        w[4] = (uint32_t)k[2], w[5] = (uint32_t)(k[2] >> 32), w[6] = (uint32_t)k[3], w[7] = (uint32_t)(k[3] >> 32);
+    }
+}
+
+template <int W>
+constexpr int btree_cx_log = W == (int)kBtreeCompressed ? 3 : 4;  // log2 of a compressed node's fanout
+
+template <int W, int kInner, bool kExact>
+GJ_DEVICE_INLINE uint32_t btree_cx_child(const btree_view& v, const uint32_t (&w)[8], uint32_t j, uint64_t span,
+                                         uint64_t key, uint64_t* B) {
+    if constexpr (W == (int)kBtreeCompressed) return btree_c7_child<kInner, kExact>(v, w, j, span, key, B);
+    else return btree_c15_child<kInner, kExact>(v, w, j, span, key, B);
+}
+
+// leaf reached for key through compressed nodes (open slots left, or exact),
+// starting at node j (base B) of level l; l = 0 means j is the leaf
+template <int W, int kInner, bool kExact>
+GJ_DEVICE_INLINE uint32_t btree_cx_descend(const btree_view& v, const uint64_t* cache, uint64_t key, int l,
+                                           uint32_t j, uint64_t B) {
+    constexpr int kLog = btree_cx_log<W>;
+    const int first_global = (int)v.height - (int)v.cached_levels;
+    uint64_t span = l >= 1 ? (uint64_t)v.leaf_keys << (kLog * (l - 1)) : 0;  // column keys under one child
+    uint32_t w[8];
+    for (; l > first_global; --l, span >>= kLog) {
+        btree_cx_node<kInner>(v, cache, l, j, true, w);
+        j = (j << kLog) + btree_cx_child<W, kInner, kExact>(v, w, j, span, key, &B);
+    }
+    for (; l >= 1; --l, span >>= kLog) {
+        btree_cx_node<kInner>(v, cache, l, j, false, w);
+        j = (j << kLog) + btree_cx_child<W, kInner, kExact>(v, w, j, span, key, &B);
     }
     return j;
 }
@@ -399,44 +416,102 @@ GJ_DEVICE_INLINE uint32_t btree_node_search(const uint64_t* node, uint64_t key, 
     }
 }
 
+// Where a descent starts: node `node` of level `level` (0: `node` is the
+// leaf), whose base is `base` (compressed nodes).
+struct btree_cursor {
+    uint64_t base;
+    uint32_t node;
+    int32_t level;
+};
+
+GJ_DEVICE_INLINE btree_cursor btree_root(const btree_view& v) { return {v.min_key, 0u, (int32_t)v.height}; }
+
+template <int W, int kInner>
+GJ_DEVICE_INLINE uint32_t btree_plain_descend(const btree_view& v, const uint64_t* cache, uint64_t key, int l,
+                                              uint32_t j) {
+    constexpr uint32_t F = W + 1;
+    // node and leaf numbers are below 2^32 (at most one leaf per key)
+    const int first_global = (int)v.height - (int)v.cached_levels;  // levels <= this come from global memory
+    for (; l > first_global; --l) j = j * F + btree_node_search<W>(cache + v.smem_offset[l] + j * W, key, true);
+    for (; l >= 1; --l) j = j * F + btree_node_search<W, kInner>(v.level[l] + (uint64_t)j * W, key, false);
+    return j;
+}
+
 // kScattered: probes arrive in random key order -- the inner levels are
 // kept in L2 over the column sectors, which are streamed.  Partitioned
 // probes (nearby keys in a row) reuse column sectors and touch only a slice
 // of the inner levels: both use the default class then.
+//
+// The search starts at `from`, a node on the key's path (the root, or the
+// deepest node shared by the paths of a run of sorted probes).
 template <int W, bool kScattered = true>
-GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
+GJ_DEVICE_INLINE uint32_t btree_lookup_from(const btree_view& v, const uint64_t* cache, uint64_t key,
+                                            const btree_cursor& from) {
     constexpr int kInner = kScattered ? kL2Keep : kL2Default;
     constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
-    if constexpr (W == (int)kBtreeCompressed || W == (int)kBtreeCompressed16) {
-        if (key > v.max_key || key < v.min_key) return kInvalid;
-        uint64_t j = btree_cx_leaf<W, kInner, false>(v, cache, key);
-        uint64_t base = j * v.leaf_keys;
-        uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
-        bool eq;
-        uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    constexpr bool kCompressed = W == (int)kBtreeCompressed || W == (int)kBtreeCompressed16;
+    if (key > v.max_key || key < v.min_key) return kInvalid;
+    uint64_t j;
+    if constexpr (kCompressed) j = btree_cx_descend<W, kInner, false>(v, cache, key, from.level, from.node, from.base);
+    else j = btree_plain_descend<W, kInner>(v, cache, key, from.level, from.node);
+    // leaf j: column slice [j*L, min(j*L + L, n))
+    uint64_t base = j * v.leaf_keys;
+    uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
+    bool eq;
+    uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    if constexpr (kCompressed) {
         if (pos == end && end < v.n) {  // a wrong left turn: search again, open slots resolved exactly
-            j = btree_cx_leaf<W, kInner, true>(v, cache, key);
+            j = btree_cx_descend<W, kInner, true>(v, cache, key, (int)v.height, 0u, v.min_key);
             base = j * v.leaf_keys;
             end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
             pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
         }
-        return eq ? (uint32_t)pos : kInvalid;
     }
-    if (key > v.max_key) return kInvalid;
-    constexpr uint32_t F = W + 1;
-    // node and leaf numbers are below 2^32 (at most one leaf per key)
-    uint32_t j = 0;
-    const int h = (int)v.height;
-    const int first_global = h - (int)v.cached_levels;  // levels <= this come from global memory
-    int l = h;
-    for (; l > first_global; --l) j = j * F + btree_node_search<W>(cache + v.smem_offset[l] + j * W, key, true);
-    for (; l >= 1; --l) j = j * F + btree_node_search<W, kInner>(v.level[l] + (uint64_t)j * W, key, false);
-    // leaf j: column slice [j*L, min(j*L + L, n))
-    const uint64_t base = (uint64_t)j * v.leaf_keys;
-    const uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
-    bool eq;
-    const uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
     return eq ? (uint32_t)pos : kInvalid;
+}
+
+template <int W, bool kScattered = true>
+GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
+    return btree_lookup_from<W, kScattered>(v, cache, key, btree_root(v));
+}
+
+// The deepest node on the paths of both lo and hi (lo <= hi): every key in
+// [lo, hi] passes through it, since the exact descent is monotonic in the
+// key.  Used once per tile of sorted probes.
+template <int W, bool kScattered = true>
+GJ_DEVICE_INLINE btree_cursor btree_common_node(const btree_view& v, const uint64_t* cache, uint64_t lo,
+                                                uint64_t hi) {
+    constexpr int kInner = kScattered ? kL2Keep : kL2Default;
+    btree_cursor c = btree_root(v);
+    lo = lo < v.min_key ? v.min_key : lo;
+    hi = hi > v.max_key ? v.max_key : hi;
+    if (lo > hi) return c;
+    const int first_global = (int)v.height - (int)v.cached_levels;
+    if constexpr (W == (int)kBtreeCompressed || W == (int)kBtreeCompressed16) {
+        constexpr int kLog = btree_cx_log<W>;
+        uint64_t span = (uint64_t)v.leaf_keys << (kLog * (c.level - 1));
+        for (; c.level >= 1; --c.level, span >>= kLog) {
+            uint32_t w[8];
+            btree_cx_node<kInner>(v, cache, c.level, c.node, c.level > first_global, w);
+            uint64_t b_lo = c.base, b_hi = c.base;
+            const uint32_t a = btree_cx_child<W, kInner, true>(v, w, c.node, span, lo, &b_lo);
+            const uint32_t b = btree_cx_child<W, kInner, true>(v, w, c.node, span, hi, &b_hi);
+            if (a != b) break;
+            c.node = (c.node << kLog) + a;
+            c.base = b_lo;
+        }
+    } else {
+        for (; c.level >= 1; --c.level) {
+            const bool sm = c.level > first_global;
+            const uint64_t* node = sm ? cache + v.smem_offset[c.level] + (uint64_t)c.node * W
+                                      : v.level[c.level] + (uint64_t)c.node * W;
+            const uint32_t a = btree_node_search<W, kInner>(node, lo, sm);
+            const uint32_t b = btree_node_search<W, kInner>(node, hi, sm);
+            if (a != b) break;
+            c.node = c.node * (W + 1) + a;
+        }
+    }
+    return c;
 }
 
 // ---------------------------------------------------------------------------
