@@ -231,7 +231,7 @@ def gpu_setup():
 def gpu_main(args):
     world, rank, device, stream = gpu_setup()
     fn = {"inlj": inlj_workload, "partitioned": partitioned_workload, "star": star_workload,
-          "learned": learned_workload, "batch": batch_workload}[args.workload]
+          "learned": learned_workload, "batch": batch_workload, "host_index": host_index_workload}[args.workload]
     line = fn(args, world, rank, device, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -461,6 +461,109 @@ def partitioned_workload(args, world, rank, device, stream):
                       "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_probe": bpp,
                       "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
          "gpu_launches": args.steps * windows * 6, "clocks": clocks, "cpu_baseline": None, "e2e": None})
+
+
+def host_memory_available() -> int:
+    """MemAvailable of /proc/meminfo in bytes (0 when unknown)."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def link_read_gbs(device, stream) -> float:
+    """Pinned host -> HBM copy bandwidth (1 GiB, best of 5): the NVLink-C2C
+    read peak the host-memory index is measured against."""
+    import torch
+
+    h = torch.empty(1 << 27, dtype=torch.int64).pin_memory()
+    d = torch.empty(1 << 27, dtype=torch.int64, device=device)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(6):
+        a.record(stream)
+        d.copy_(h, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b)
+        best = t if best is None or t < best else best
+    del h, d
+    return (8 << 27) / (best / 1e3) / 1e9
+
+
+def host_index_workload(args, world, rank, device, stream):
+    """Index resident in pinned Grace memory, read by the probe kernels over
+    NVLink-C2C -- the GB300 form of the reference's index in host memory over
+    NVLink 2.0 (src/index_lookup_config.hpp:52-66).  The column and the index
+    live on the host, probes and pairs in HBM; the same data with the index in
+    HBM runs beside it.  Column sizes that would take more than a quarter of
+    the host's available memory are skipped."""
+    import ctypes
+
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    m = 1 << args.m_log2
+    kind = args.indexes.split(",")[0]
+    params = index_params(args, kind)
+    avail = host_memory_available()
+    link = link_read_gbs(device, stream)
+    pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device)
+    wsz = ctypes.c_size_t(0)
+    gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(wsz))
+    ws = torch.empty(wsz.value, dtype=torch.uint8, device=device)
+    sizes, head = {}, None
+    for nl in [int(x) for x in args.host_n_log2.split(",")]:
+        n = 1 << nl
+        if avail and 8 * n * 1.25 > avail // 4:
+            sizes[f"2^{nl}"] = {"skipped": f"{8 * n} B column against {avail} B of available host memory"}
+            continue
+        keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
+        probes = gj.generate_probes(keys, m, theta=args.theta, seed=args.seed + 1)
+        h_keys = torch.empty(n, dtype=torch.int64, pin_memory=True)
+        h_keys.copy_(keys)
+        torch.cuda.synchronize()
+        row = {}
+        for placement in ("host", "device"):
+            if placement == "host":
+                ix = gj.make_index(kind, index_memory=gj.INDEX_MEMORY_HOST, **params).construct(None, h_keys)
+            else:
+                ix = gj.make_index(kind, **params).construct(None, keys)
+            ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, ws), args.steps, args.warmup, stream,
+                            world, device)
+            ms = max_over_ranks(ms, world, device)
+            row[placement] = {"tuples_per_s": world * m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                              "pairs": int(count.item()), "index_bytes": ix.memory_consumption(),
+                              "host_index_bytes": ix.host_memory()}
+            ix.free()
+        row["same_pairs"] = row["host"]["pairs"] == row["device"]["pairs"]
+        sizes[f"2^{nl}"] = row
+        head = head or (nl, row)
+        del keys, probes, h_keys
+        torch.cuda.empty_cache()
+    if head is None:
+        return {"metric": "INLJ probe tuples/s, index in host memory", "unavailable": "no column size fits"}
+    nl, row = head
+    per_step = row["host"]["ms_per_step"]
+    # over the link per probe: the column sector that holds the answer (the
+    # column is read from host memory; upper index levels stay in L2)
+    link_bytes = 32
+    achieved = link_bytes * m / (per_step / 1e3) / 1e9
+    return _base_line(
+        args, world, f"INLJ probe tuples/s ({kind} in host memory over NVLink-C2C, 1 GB300 per rank)",
+        row["host"]["tuples_per_s"], "probe tuples/s", per_step,
+        f"INLJ pairs, index and 2^{nl}-key column in pinned host memory, {m} Zipf({args.theta}) probes in HBM",
+        {"host_index": {"index": kind, "params": params, "sizes": sizes, "host_memory_available": avail},
+         "roofline": {"bound": "nvlink-c2c", "achieved": round(achieved, 1), "peak": round(link, 1), "unit": "GB/s",
+                      "frac": round(achieved / link, 4), "traffic": None, "link_bytes_per_probe": link_bytes,
+                      "peak_source": "pinned host-to-device copy measured in this run"},
+         "gpu_launches": 2 * args.steps, "cpu_baseline": None, "e2e": None})
 
 
 def star_inputs(n_fact, n_dim, seed, device):
@@ -706,7 +809,9 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch"], default="inlj")
+    ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch", "host_index"],
+                    default="inlj")
+    ap.add_argument("--host-n-log2", default="26,28", help="host_index: column sizes (log2 keys)")
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)
     ap.add_argument("--theta", type=float, default=0.5)

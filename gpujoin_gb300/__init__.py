@@ -78,8 +78,15 @@ class gj_index_params(ctypes.Structure):
         ("learned_steps", ctypes.c_uint32),
         ("learned_batch", ctypes.c_uint32),
         ("learned_lr", ctypes.c_float),
+        ("index_memory", ctypes.c_uint32),
+        ("reserved0", ctypes.c_uint32),
         ("seed", ctypes.c_uint64),
     ]
+
+
+# gj_index_params.index_memory
+INDEX_MEMORY_DEVICE = 0
+INDEX_MEMORY_HOST = 1
 
 
 _LIB: Optional[ctypes.CDLL] = None
@@ -98,6 +105,7 @@ _SIGNATURES = {
     "gj_index_build": (_i32, [_i32, _vp, _vp, _u64, ctypes.POINTER(gj_index_params), _vp, ctypes.POINTER(_vp)]),
     "gj_index_free": (_i32, [_vp]),
     "gj_index_memory_consumption": (_u64, [_vp]),
+    "gj_index_host_memory": (_u64, [_vp]),
     "gj_index_get_type": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "gj_index_size": (_u64, [_vp]),
     "gj_index_learned_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)]),
@@ -239,9 +247,14 @@ class abstract_index:
 
     # construct(h_column, d_column) -- src/indexes.cuh:36
     def construct(self, h_column, d_column, stream=None) -> "abstract_index":
+        """d_column: the sorted keys as a CUDA tensor, or, for an index built with
+        index_memory=INDEX_MEMORY_HOST, as a pinned host tensor (read over NVLink-C2C)."""
         torch = _torch()
-        if d_column is None or not d_column.is_cuda:
-            raise ValueError("d_column must be a CUDA tensor")
+        host_index = self.params.index_memory == INDEX_MEMORY_HOST
+        if d_column is None or not (d_column.is_cuda or (host_index and d_column.is_pinned())):
+            raise ValueError("d_column must be a CUDA tensor (or a pinned host tensor for a host-memory index)")
+        if not d_column.is_contiguous():
+            raise ValueError("d_column must be contiguous")
         if d_column.dtype not in (torch.int64, getattr(torch, "uint64", torch.int64)):
             raise ValueError("d_column must hold 64-bit keys")
         self.free()
@@ -251,8 +264,8 @@ class abstract_index:
 
             self._h_column = np.ascontiguousarray(h_column, dtype=np.uint64)
             h_ptr = self._h_column.ctypes.data
-        with torch.cuda.device(d_column.device):
-            _check(lib().gj_index_build(int(self.index_type), _ptr(d_column), h_ptr, d_column.numel(),
+        with torch.cuda.device(d_column.device if d_column.is_cuda else torch.cuda.current_device()):
+            _check(lib().gj_index_build(int(self.index_type), d_column.data_ptr(), h_ptr, d_column.numel(),
                                         ctypes.byref(self.params), _stream(stream), ctypes.byref(self._handle)))
         self.d_column = d_column
         self._h_column = None
@@ -261,6 +274,10 @@ class abstract_index:
     def memory_consumption(self) -> int:
         """src/indexes.cuh:38"""
         return int(lib().gj_index_memory_consumption(self._handle))
+
+    def host_memory(self) -> int:
+        """Bytes of the index's own arrays in pinned host memory (index_memory=INDEX_MEMORY_HOST)."""
+        return int(lib().gj_index_host_memory(self._handle))
 
     @property
     def handle(self) -> int:

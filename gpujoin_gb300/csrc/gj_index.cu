@@ -164,8 +164,22 @@ __global__ void k_encode_btree_c15(const uint64_t* __restrict__ col, uint64_t n,
     }
 }
 
+// storage of the index's own arrays: HBM, or pinned host memory that the
+// kernels read through its device mapping (the same address under unified
+// addressing)
 int device_alloc(gj_index* idx, size_t bytes, void** out) {
     void* p = nullptr;
+    if (idx->params.index_memory == GJ_INDEX_MEMORY_HOST) {
+        const cudaError_t e = cudaHostAlloc(&p, bytes ? bytes : 16, cudaHostAllocMapped);
+        if (e != cudaSuccess) {
+            set_error("cudaHostAlloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? GJ_ERR_OUT_OF_MEMORY : GJ_ERR_CUDA;
+        }
+        idx->host_allocations.push_back(p);
+        idx->host_bytes += bytes;
+        *out = p;
+        return GJ_OK;
+    }
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
         set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
@@ -185,7 +199,7 @@ int host_copy_of_column(const uint64_t* d_keys, const uint64_t* h_keys, uint64_t
         return GJ_OK;
     }
     store->resize(n);
-    GJ_CUDA_TRY(cudaMemcpy(store->data(), d_keys, n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    GJ_CUDA_TRY(cudaMemcpy(store->data(), d_keys, n * sizeof(uint64_t), cudaMemcpyDefault));
     *out = store->data();
     return GJ_OK;
 }
@@ -254,7 +268,7 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     GJ_TRY(device_alloc(idx, total * sizeof(uint64_t), &p));
     uint64_t* base = static_cast<uint64_t*>(p);
     uint64_t min_key = 0;
-    GJ_CUDA_TRY(cudaMemcpyAsync(&min_key, idx->d_col, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(&min_key, idx->d_col, sizeof(uint64_t), cudaMemcpyDefault, s));
     if (compressed) {
         // top down: a node's base comes from its parent's encoding
         uint64_t* bases[2] = {nullptr, nullptr};
@@ -325,7 +339,7 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     idx->bt.leaf_keys = L;
     idx->bt.col_aligned = aligned32(idx->d_col);
     uint64_t maxk = 0;
-    GJ_CUDA_TRY(cudaMemcpyAsync(&maxk, idx->d_col + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(&maxk, idx->d_col + n - 1, sizeof(uint64_t), cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     idx->bt.max_key = maxk;
     idx->bt.min_key = min_key;
@@ -348,8 +362,8 @@ int build_harmonia(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
     GJ_TRY(device_alloc(idx, ha.keys.size() * sizeof(uint64_t), &pk));
     GJ_TRY(device_alloc(idx, ha.children.size() * sizeof(uint64_t), &pc));
     if (!ha.keys.empty())
-        GJ_CUDA_TRY(cudaMemcpyAsync(pk, ha.keys.data(), ha.keys.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(pc, ha.children.data(), ha.children.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(pk, ha.keys.data(), ha.keys.size() * sizeof(uint64_t), cudaMemcpyDefault, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(pc, ha.children.data(), ha.children.size() * sizeof(uint64_t), cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     idx->hm.keys = static_cast<uint64_t*>(pk);
     idx->hm.children = static_cast<uint64_t*>(pc);
@@ -383,9 +397,9 @@ int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t
     GJ_TRY(device_alloc(idx, rs.table.size() * sizeof(uint32_t), &pt));
     GJ_TRY(device_alloc(idx, rs.sx.size() * sizeof(uint64_t), &px));
     GJ_TRY(device_alloc(idx, rs.sy.size() * sizeof(double), &py));
-    GJ_CUDA_TRY(cudaMemcpyAsync(pt, rs.table.data(), rs.table.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(px, rs.sx.data(), rs.sx.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(py, rs.sy.data(), rs.sy.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(pt, rs.table.data(), rs.table.size() * sizeof(uint32_t), cudaMemcpyDefault, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(px, rs.sx.data(), rs.sx.size() * sizeof(uint64_t), cudaMemcpyDefault, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(py, rs.sy.data(), rs.sy.size() * sizeof(double), cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     idx->rs.col = idx->d_col;
     idx->rs.n = idx->n;
@@ -494,6 +508,8 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
         GJ_CHECK_ARG(params->struct_size == sizeof(gj_index_params), "gj_index_build: params.struct_size mismatch");
         p = *params;
     }
+    GJ_CHECK_ARG(p.index_memory == GJ_INDEX_MEMORY_DEVICE || p.index_memory == GJ_INDEX_MEMORY_HOST,
+                 "gj_index_build: index_memory must be GJ_INDEX_MEMORY_DEVICE or GJ_INDEX_MEMORY_HOST");
     cudaStream_t s = as_stream(stream);
     std::unique_ptr<gj_index> idx(new gj_index());
     idx->type = type;
@@ -519,8 +535,8 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
     }
     if (n > 0 && d_keys) {
         // key range, kept on the host (partition functions need it per call)
-        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->min_key, d_keys, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->max_key, d_keys + n - 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->min_key, d_keys, sizeof(uint64_t), cudaMemcpyDefault, s));
+        GJ_CUDA_TRY(cudaMemcpyAsync(&idx->max_key, d_keys + n - 1, sizeof(uint64_t), cudaMemcpyDefault, s));
         GJ_CUDA_TRY(cudaStreamSynchronize(s));
     }
 
@@ -542,6 +558,7 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
     }
     if (rc != GJ_OK) {
         for (void* a : idx->allocations) cudaFree(a);
+        for (void* a : idx->host_allocations) cudaFreeHost(a);
         return rc;
     }
     *out_index = idx.release();
@@ -561,12 +578,21 @@ int gj_index_free(gj_index* index) {
             rc = GJ_ERR_CUDA;
         }
     }
+    for (void* a : index->host_allocations) {
+        cudaError_t e = cudaFreeHost(a);
+        if (e != cudaSuccess && rc == GJ_OK) {
+            set_error("cudaFreeHost: %s", cudaGetErrorString(e));
+            rc = GJ_ERR_CUDA;
+        }
+    }
     if (prev != index->device && prev >= 0) cudaSetDevice(prev);
     delete index;
     return rc;
 }
 
 uint64_t gj_index_memory_consumption(const gj_index* index) { return index ? index->bytes : 0; }
+
+uint64_t gj_index_host_memory(const gj_index* index) { return index ? index->host_bytes : 0; }
 
 int gj_index_get_type(const gj_index* index, int* out_type) {
     GJ_CHECK_ARG(index && out_type, "gj_index_get_type: null argument");

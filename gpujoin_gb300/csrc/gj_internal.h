@@ -105,8 +105,10 @@ struct gj_index {
     const uint64_t* d_col = nullptr;
     uint64_t min_key = 0, max_key = 0;  // d_col[0], d_col[n - 1] (0 when empty)
     uint64_t bytes = 0;  // memory_consumption
+    uint64_t host_bytes = 0;  // of which in pinned host memory
     gj_index_params params{};
-    std::vector<void*> allocations;  // owned device memory
+    std::vector<void*> allocations;       // owned device memory
+    std::vector<void*> host_allocations;  // owned pinned host memory (index_memory = host)
 
     gj::bs_view bs{};
     gj::btree_view bt{};

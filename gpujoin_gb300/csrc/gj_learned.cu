@@ -384,8 +384,8 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         return GJ_ERR_INVALID_ARGUMENT;
     }
     uint64_t ends[2] = {0, 0};
-    GJ_CUDA_TRY(cudaMemcpyAsync(&ends[0], idx->d_col, 8, cudaMemcpyDeviceToHost, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(&ends[1], idx->d_col + n - 1, 8, cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(&ends[0], idx->d_col, 8, cudaMemcpyDefault, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(&ends[1], idx->d_col + n - 1, 8, cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     learned_view& v = idx->ln;
     v.col = idx->d_col;
@@ -515,7 +515,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         }
         out[4 * W + W * W] = best[4 * H + H * H];  // b3
     }
-    GJ_CUDA_TRY(cudaMemcpyAsync(d_root, idx->ln_root.w, nstored * sizeof(float), cudaMemcpyHostToDevice, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(d_root, idx->ln_root.w, nstored * sizeof(float), cudaMemcpyDefault, s));
 
     // route every key, fit the leaves, measure their error windows
     uint32_t* leaf_of = nullptr;
@@ -536,7 +536,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     // statistics: largest window and key-weighted mean window
     std::vector<learned_leaf> hl(L);
     std::vector<unsigned int> hc(L);
-    GJ_CUDA_TRY(cudaMemcpyAsync(hl.data(), v.leaves, L * sizeof(learned_leaf), cudaMemcpyDeviceToHost, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(hl.data(), v.leaves, L * sizeof(learned_leaf), cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaMemcpyAsync(hc.data(), count, L * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     uint64_t max_err = 0;

@@ -57,6 +57,12 @@ typedef enum gj_index_type {
 } gj_index_type;
 
 /* learned root models */
+/* gj_index_params.index_memory.  The reference keeps its index in host
+ * memory read over NVLink 2.0 (src/index_lookup_config.hpp:52-66); on GB300
+ * that is pinned Grace memory read over NVLink-C2C. */
+#define GJ_INDEX_MEMORY_DEVICE 0u
+#define GJ_INDEX_MEMORY_HOST 1u
+
 #define GJ_LEARNED_ROOT_LINEAR 0u
 #define GJ_LEARNED_ROOT_MLP 1u
 
@@ -81,6 +87,10 @@ typedef struct gj_index_params {
     uint32_t learned_steps;     /* root training steps (default 600) */
     uint32_t learned_batch;     /* root training batch (default 8192) */
     float learned_lr;           /* root learning rate (Adam, default 1e-3) */
+    uint32_t index_memory;      /* where the index's own arrays live: GJ_INDEX_MEMORY_DEVICE (HBM, default)
+                                   or GJ_INDEX_MEMORY_HOST (pinned Grace memory, read by the kernels over
+                                   NVLink-C2C; pair it with a column in pinned host memory) */
+    uint32_t reserved0;         /* 0 */
     uint64_t seed;              /* training / sampling seed */
 } gj_index_params;
 
@@ -111,6 +121,9 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
 int gj_index_free(gj_index* index);
 /* abstract_index::memory_consumption (src/indexes.cuh:38) in bytes */
 uint64_t gj_index_memory_consumption(const gj_index* index);
+/* bytes of the index's own arrays that live in pinned host memory
+ * (index_memory = GJ_INDEX_MEMORY_HOST); 0 for an index in HBM */
+uint64_t gj_index_host_memory(const gj_index* index);
 int gj_index_get_type(const gj_index* index, int* out_type);
 uint64_t gj_index_size(const gj_index* index);
 /* learned index: recorded maximum prediction error (positions) and mean
