@@ -530,9 +530,13 @@ def host_index_workload(args, world, rank, device, stream):
         h_keys.copy_(keys)
         torch.cuda.synchronize()
         row = {}
-        for placement in ("host", "device"):
+        # host: column and index in Grace memory (the reference's setting);
+        # column_host: column in Grace memory, inner levels in HBM; device: HBM
+        for placement in ("host", "column_host", "device"):
             if placement == "host":
                 ix = gj.make_index(kind, index_memory=gj.INDEX_MEMORY_HOST, **params).construct(None, h_keys)
+            elif placement == "column_host":
+                ix = gj.make_index(kind, **params).construct(None, h_keys)
             else:
                 ix = gj.make_index(kind, **params).construct(None, keys)
             ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, ws), args.steps, args.warmup, stream,
@@ -542,7 +546,7 @@ def host_index_workload(args, world, rank, device, stream):
                               "pairs": int(count.item()), "index_bytes": ix.memory_consumption(),
                               "host_index_bytes": ix.host_memory()}
             ix.free()
-        row["same_pairs"] = row["host"]["pairs"] == row["device"]["pairs"]
+        row["same_pairs"] = row["host"]["pairs"] == row["device"]["pairs"] == row["column_host"]["pairs"]
         sizes[f"2^{nl}"] = row
         head = head or (nl, row)
         del keys, probes, h_keys
@@ -550,15 +554,16 @@ def host_index_workload(args, world, rank, device, stream):
     if head is None:
         return {"metric": "INLJ probe tuples/s, index in host memory", "unavailable": "no column size fits"}
     nl, row = head
-    per_step = row["host"]["ms_per_step"]
+    per_step = row["column_host"]["ms_per_step"]
     # over the link per probe: the column sector that holds the answer (the
-    # column is read from host memory; upper index levels stay in L2)
+    # inner levels stay in HBM / L2)
     link_bytes = 32
     achieved = link_bytes * m / (per_step / 1e3) / 1e9
     return _base_line(
-        args, world, f"INLJ probe tuples/s ({kind} in host memory over NVLink-C2C, 1 GB300 per rank)",
-        row["host"]["tuples_per_s"], "probe tuples/s", per_step,
-        f"INLJ pairs, index and 2^{nl}-key column in pinned host memory, {m} Zipf({args.theta}) probes in HBM",
+        args, world, f"INLJ probe tuples/s ({kind}, column in Grace memory over NVLink-C2C, 1 GB300 per rank)",
+        row["column_host"]["tuples_per_s"], "probe tuples/s", per_step,
+        f"INLJ pairs, 2^{nl}-key column in pinned host memory, index levels in HBM, {m} Zipf({args.theta}) "
+        f"probes in HBM (sizes: column and index in host memory / column in host memory / all in HBM)",
         {"host_index": {"index": kind, "params": params, "sizes": sizes, "host_memory_available": avail},
          "roofline": {"bound": "nvlink-c2c", "achieved": round(achieved, 1), "peak": round(link, 1), "unit": "GB/s",
                       "frac": round(achieved / link, 4), "traffic": None, "link_bytes_per_probe": link_bytes,
@@ -815,7 +820,7 @@ def parse_args(argv=None):
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)
     ap.add_argument("--theta", type=float, default=0.5)
-    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned")
+    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned,hash")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample", type=int, default=1 << 28,
                     help="probes of the CPU baseline leg (one timed pass; about 6 s on 16 Grace cores)")

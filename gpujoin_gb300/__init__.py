@@ -61,6 +61,7 @@ class index_type_enum(enum.IntEnum):
     radix_spline = 3
     no_op = 4
     learned = 5
+    hash = 6
 
 
 class gj_index_params(ctypes.Structure):
@@ -247,12 +248,12 @@ class abstract_index:
 
     # construct(h_column, d_column) -- src/indexes.cuh:36
     def construct(self, h_column, d_column, stream=None) -> "abstract_index":
-        """d_column: the sorted keys as a CUDA tensor, or, for an index built with
-        index_memory=INDEX_MEMORY_HOST, as a pinned host tensor (read over NVLink-C2C)."""
+        """d_column: the sorted keys as a CUDA tensor or as a pinned host tensor
+        (Grace memory, read by the kernels over NVLink-C2C).  Where the index's
+        own arrays live is the index_memory parameter (HBM by default)."""
         torch = _torch()
-        host_index = self.params.index_memory == INDEX_MEMORY_HOST
-        if d_column is None or not (d_column.is_cuda or (host_index and d_column.is_pinned())):
-            raise ValueError("d_column must be a CUDA tensor (or a pinned host tensor for a host-memory index)")
+        if d_column is None or not (d_column.is_cuda or d_column.is_pinned()):
+            raise ValueError("d_column must be a CUDA tensor or a pinned host tensor")
         if not d_column.is_contiguous():
             raise ValueError("d_column must be contiguous")
         if d_column.dtype not in (torch.int64, getattr(torch, "uint64", torch.int64)):
@@ -429,6 +430,13 @@ class learned_index(abstract_index):
         return int(me.value), float(mw.value)
 
 
+class hash_index(abstract_index):
+    """The reference's hash-join table (src/linear_probing_hashtable.cuh) as an index: linear probing,
+    load factor <= 0.5; position of the equal key, else GJ_INVALID_POS."""
+
+    index_type = index_type_enum.hash
+
+
 _INDEX_CLASSES = {
     index_type_enum.btree: btree_index,
     index_type_enum.harmonia: harmonia_index,
@@ -436,6 +444,7 @@ _INDEX_CLASSES = {
     index_type_enum.radix_spline: radix_spline_index,
     index_type_enum.no_op: no_op_index,
     index_type_enum.learned: learned_index,
+    index_type_enum.hash: hash_index,
 }
 
 

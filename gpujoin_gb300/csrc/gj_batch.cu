@@ -41,6 +41,7 @@ struct any_view {
         harmonia_view hm;
         rs_view rs;
         learned_view ln;
+        hash_view hs;
     } u;
 };
 static_assert(sizeof(any_view) % 4 == 0, "views are staged as 32-bit words");
@@ -75,6 +76,7 @@ __device__ __forceinline__ uint32_t any_lookup(const any_view& v, const float* r
         case GJ_INDEX_HARMONIA: return harmonia_lookup(v.u.hm, nullptr, key);
         case GJ_INDEX_RADIX_SPLINE: return rs_lookup(v.u.rs, key);
         case GJ_INDEX_LEARNED: return learned_lookup(v.u.ln, root, key);
+        case GJ_INDEX_HASH: return hash_lookup(v.u.hs, key);
         default: return kInvalid;
     }
 }
@@ -344,6 +346,7 @@ int gj_batch_plan_create(gj_index* const* indexes, uint32_t num_indexes, const u
             case GJ_INDEX_HARMONIA: v.u.hm = ix->hm; v.u.hm.cached_nodes = 0; v.u.hm.cached_levels = 0; break;
             case GJ_INDEX_RADIX_SPLINE: v.u.rs = ix->rs; break;
             case GJ_INDEX_LEARNED: v.u.ln = ix->ln; break;
+            case GJ_INDEX_HASH: v.u.hs = ix->hs; break;
             default: break;
         }
     }

@@ -131,9 +131,9 @@ __global__ void k_encode_btree_c7(const uint64_t* __restrict__ col, uint64_t n, 
     }
 }
 
-// nodes of 16 lanes of 16 bits (node width 15): lane 0 = shift, lanes 1..15 =
-// separators (rounded down) relative to the node's base, at most
-// kBtreeMaxDelta16, kBtreeAbsent16 past the column's end
+// nodes of 16 lanes of 16 bits (node width 15): lane 0 = header | shift,
+// lanes 1..15 = bias | separator (rounded down) relative to the node's base,
+// the delta at most kBtreeMaxDelta16; kBtreeAbsent16 past the column's end
 __global__ void k_encode_btree_c15(const uint64_t* __restrict__ col, uint64_t n, uint64_t span, uint64_t nodes,
                                    const uint16_t* __restrict__ parent, const uint64_t* __restrict__ parent_base,
                                    uint64_t min_key, uint64_t* __restrict__ base_out, uint16_t* __restrict__ out) {
@@ -142,21 +142,21 @@ __global__ void k_encode_btree_c15(const uint64_t* __restrict__ col, uint64_t n,
         if (parent) {
             const uint64_t p = j >> 4, c = j & 15;
             B = parent_base[p];
-            if (c) B += (uint64_t)parent[p * 16 + c] << (parent[p * 16] & 63u);
+            if (c) B += (uint64_t)(parent[p * 16 + c] & 0x7FFFu) << (parent[p * 16] & 63u);
         }
         base_out[j] = B;
         const uint64_t end = (j + 1) * 16 * span < n ? (j + 1) * 16 * span : n;
         const uint64_t range = col[end - 1] - B;
         const unsigned bits = range ? 64u - (unsigned)__clzll(range) : 0u;
-        uint32_t sh = bits > 15 ? bits - 15 : 0;
+        uint32_t sh = bits > 14 ? bits - 14 : 0;
         if ((range >> sh) > kBtreeMaxDelta16) sh += 1;
         uint16_t* w = out + j * 16;
-        w[0] = (uint16_t)sh;
+        w[0] = (uint16_t)(kBtreeHeader16 | sh);
         for (uint32_t i = 0; i < 15; ++i) {
             const uint64_t first = (j * 16 + i) * span;
             if (first < n) {
                 const uint64_t last = first + span < n ? first + span : n;
-                w[i + 1] = (uint16_t)((col[last - 1] - B) >> sh);
+                w[i + 1] = (uint16_t)(kBtreeLaneBias16 | ((col[last - 1] - B) >> sh));
             } else {
                 w[i + 1] = (uint16_t)kBtreeAbsent16;
             }
@@ -167,6 +167,32 @@ __global__ void k_encode_btree_c15(const uint64_t* __restrict__ col, uint64_t n,
 // storage of the index's own arrays: HBM, or pinned host memory that the
 // kernels read through its device mapping (the same address under unified
 // addressing)
+__global__ void k_hash_clear(hash_slot* slots, uint64_t capacity) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < capacity;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        slots[i] = hash_slot{~0ull, kHashEmpty, 0u};
+}
+
+// insert (src/linear_probing_hashtable.cuh:36-46): claim the first free slot
+// from the key's home slot on; the keys are unique, so no slot is matched
+__global__ void k_hash_insert(const uint64_t* __restrict__ col, uint64_t n, hash_slot* slots, uint64_t mask,
+                              unsigned int* full) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = col[i];
+        uint64_t h = murmur3_fmix64(key) & mask;
+        bool placed = false;
+        for (uint64_t step = 0; step <= mask; ++step) {
+            if (atomicCAS(&slots[h].pos, kHashEmpty, (uint32_t)i) == kHashEmpty) {
+                slots[h].key = key;
+                placed = true;
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+        if (!placed) atomicExch(full, 1u);
+    }
+}
+
 int device_alloc(gj_index* idx, size_t bytes, void** out) {
     void* p = nullptr;
     if (idx->params.index_memory == GJ_INDEX_MEMORY_HOST) {
@@ -415,6 +441,57 @@ int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t
     return GJ_OK;
 }
 
+// hash table over the column; built in HBM and copied when the index lives in
+// host memory (atomics stay on the device)
+int build_hash(gj_index* idx, cudaStream_t s) {
+    const uint64_t n = idx->n;
+    uint64_t capacity = 2;
+    while (capacity < 2 * n) capacity <<= 1;
+    const size_t bytes = capacity * sizeof(hash_slot);
+    void* p = nullptr;
+    GJ_TRY(device_alloc(idx, bytes, &p));
+    const bool host = idx->params.index_memory == GJ_INDEX_MEMORY_HOST;
+    hash_slot* table = static_cast<hash_slot*>(p);
+    unsigned int* full = nullptr;
+    if (host) {
+        const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&table), bytes);
+        if (e != cudaSuccess) {
+            set_error("hash: scratch table of %zu bytes: %s", bytes, cudaGetErrorString(e));
+            return GJ_ERR_OUT_OF_MEMORY;
+        }
+    }
+    int rc = GJ_OK;
+    if (cudaMalloc(reinterpret_cast<void**>(&full), sizeof(unsigned int)) != cudaSuccess) {
+        set_error("hash: flag allocation failed");
+        rc = GJ_ERR_OUT_OF_MEMORY;
+    }
+    unsigned int h_full = 0;
+    if (rc == GJ_OK) {
+        cudaMemsetAsync(full, 0, sizeof(unsigned int), s);
+        k_hash_clear<<<(int)std::min<uint64_t>((capacity + 255) / 256, 65535), 256, 0, s>>>(table, capacity);
+        k_hash_insert<<<(int)std::min<uint64_t>((n + 255) / 256, 65535), 256, 0, s>>>(idx->d_col, n, table,
+                                                                                      capacity - 1, full);
+        if (host) cudaMemcpyAsync(p, table, bytes, cudaMemcpyDefault, s);
+        cudaMemcpyAsync(&h_full, full, sizeof(h_full), cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("hash: build failed: %s", cudaGetErrorString(e));
+            rc = GJ_ERR_CUDA;
+        } else if (h_full) {
+            set_error("hash: table full");
+            rc = GJ_ERR_CUDA;
+        }
+    }
+    cudaFree(full);
+    if (host) cudaFree(table);
+    GJ_TRY(rc);
+    idx->hs.slots = static_cast<const hash_slot*>(p);
+    idx->hs.mask = capacity - 1;
+    idx->hs.n = n;
+    idx->bytes = bytes;
+    return GJ_OK;
+}
+
 }  // namespace
 
 int build_learned(gj_index* idx, cudaStream_t s);  // gj_learned.cu
@@ -465,7 +542,8 @@ int gj_parse_index_type(const char* name, int* out_type) {
                  {"binary_search", GJ_INDEX_BINARY_SEARCH},
                  {"radix_spline", GJ_INDEX_RADIX_SPLINE},
                  {"no_op", GJ_INDEX_NO_OP},
-                 {"learned", GJ_INDEX_LEARNED}};
+                 {"learned", GJ_INDEX_LEARNED},
+                 {"hash", GJ_INDEX_HASH}};
     for (const auto& e : table) {
         if (std::strcmp(name, e.name) == 0) {
             *out_type = e.type;
@@ -484,6 +562,7 @@ const char* gj_index_type_name(int type) {
         case GJ_INDEX_RADIX_SPLINE: return "radix_spline";
         case GJ_INDEX_NO_OP: return "no_op";
         case GJ_INDEX_LEARNED: return "learned";
+        case GJ_INDEX_HASH: return "hash";
         default: return nullptr;
     }
 }
@@ -547,6 +626,7 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
         case GJ_INDEX_HARMONIA: rc = build_harmonia(idx.get(), h_keys, s); break;
         case GJ_INDEX_RADIX_SPLINE: rc = build_radix_spline_index(idx.get(), h_keys, s); break;
         case GJ_INDEX_LEARNED: rc = build_learned(idx.get(), s); break;
+        case GJ_INDEX_HASH: rc = build_hash(idx.get(), s); break;
         case GJ_INDEX_NO_OP: break;
     }
     if (rc == GJ_OK) {
@@ -639,6 +719,7 @@ int gj_index_device_view(const gj_index* index, void* view, size_t view_bytes) {
         }
         case GJ_INDEX_RADIX_SPLINE: return copy(&index->rs, sizeof(index->rs));
         case GJ_INDEX_LEARNED: return copy(&index->ln, sizeof(index->ln));
+        case GJ_INDEX_HASH: return copy(&index->hs, sizeof(index->hs));
         default: return copy(nullptr, 0);
     }
 }

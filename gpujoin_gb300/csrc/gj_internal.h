@@ -115,6 +115,7 @@ struct gj_index {
     gj::harmonia_view hm{};
     gj::rs_view rs{};
     gj::learned_view ln{};
+    gj::hash_view hs{};
     gj::learned_root_params ln_root{};  // host copy of the root parameters (kernel arguments)
     uint64_t learned_max_error = 0;
     double learned_mean_window = 0.0;

@@ -1,12 +1,13 @@
 // gj_lookup.cu -- the library's entry to the probe kernels: dispatch over
 // the index kind to the unit that compiles its kernels, and the kinds
-// compiled here (binary search, no-op).  Kernels: gj_lookup_kernels.cuh.
+// compiled here (binary search, hash table, no-op).  Kernels: gj_lookup_kernels.cuh.
 #include "gj_lookup_kernels.cuh"
 
 namespace gj {
 
 int lookup_call_bs(const gj_index* idx, const lookup_call& c) { return run_call(op_bs{idx->bs}, idx, c); }
 int lookup_call_noop(const gj_index* idx, const lookup_call& c) { return run_call(op_noop{}, idx, c); }
+int lookup_call_hash(const gj_index* idx, const lookup_call& c) { return run_call(op_hash{idx->hs}, idx, c); }
 
 namespace {
 
@@ -20,6 +21,7 @@ int dispatch(const gj_index* idx, const lookup_call& c) {
         case GJ_INDEX_RADIX_SPLINE: return lookup_call_rs(idx, c);
         case GJ_INDEX_LEARNED: return lookup_call_learned(idx, c);
         case GJ_INDEX_NO_OP: return lookup_call_noop(idx, c);
+        case GJ_INDEX_HASH: return lookup_call_hash(idx, c);
         default: set_error("unknown index type %d", idx->type); return GJ_ERR_INVALID_ARGUMENT;
     }
 }

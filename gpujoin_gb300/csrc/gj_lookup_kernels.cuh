@@ -46,6 +46,7 @@ int lookup_call_noop(const gj_index* idx, const lookup_call& c);
 int lookup_call_harmonia(const gj_index* idx, const lookup_call& c);
 int lookup_call_rs(const gj_index* idx, const lookup_call& c);
 int lookup_call_learned(const gj_index* idx, const lookup_call& c);
+int lookup_call_hash(const gj_index* idx, const lookup_call& c);
 template <int W>
 int lookup_call_btree(const gj_index* idx, const lookup_call& c);  // the widths of btree_dispatch:
 template <> int lookup_call_btree<4>(const gj_index* idx, const lookup_call& c);
@@ -140,6 +141,15 @@ struct op_rs {
     template <bool kScattered = true>
     __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
         return rs_lookup<kScattered>(v, key);
+    }
+    __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
+};
+struct op_hash {
+    static constexpr int kMinBlocks = GJ_BLOCKS(8);
+    hash_view v;
+    template <bool kScattered = true>
+    __device__ __forceinline__ uint32_t lookup(const uint64_t*, uint64_t key) const {
+        return hash_lookup(v, key);
     }
     __device__ __forceinline__ uint32_t operator()(const uint64_t* cache, uint64_t key) const { return lookup(cache, key); }
 };

@@ -53,7 +53,9 @@ typedef enum gj_index_type {
     GJ_INDEX_BINARY_SEARCH = 2,
     GJ_INDEX_RADIX_SPLINE = 3,
     GJ_INDEX_NO_OP = 4,
-    GJ_INDEX_LEARNED = 5 /* not in the reference: trained position model */
+    GJ_INDEX_LEARNED = 5, /* not in the reference: trained position model */
+    GJ_INDEX_HASH = 6     /* the reference's hash-join table (src/linear_probing_hashtable.cuh) as an index:
+                             position of the equal key, else GJ_INVALID_POS */
 } gj_index_type;
 
 /* learned root models */
@@ -74,7 +76,7 @@ typedef struct gj_index_params {
     uint32_t btree_node_keys;   /* separators per B+tree inner node (fanout - 1): 4, 8, 16, 32 or 64 uint64
                                    separators, or a compressed node of one 32-byte sector holding its
                                    separators as deltas from a base the search carries: 7 (32-bit deltas,
-                                   fanout 8) or 15 (default; 15-bit deltas, fanout 16) */
+                                   fanout 8) or 15 (default; 14-bit deltas, fanout 16) */
     uint32_t btree_leaf_keys;   /* keys per B+tree leaf (column slice), a power of two <= 4096 (default 4:
                                    one 32-byte sector) */
     uint32_t rs_radix_bits;     /* RadixSpline radix table bits (default 18) */

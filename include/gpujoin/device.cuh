@@ -287,19 +287,23 @@ GJ_DEVICE_INLINE uint32_t btree_c7_child(const btree_view& v, const uint32_t (&w
     return c;
 }
 
-// Compressed nodes of 16 lanes (node width 15): lane 0 = shift s, lanes
-// 1..15 = separators as (separator - B) >> s, at most kBtreeMaxDelta16;
-// kBtreeAbsent16 past the column's end.  Lane i sits in word i / 2, low half
-// for even i.  Every lane is below 2^15, so one 32-bit subtraction compares
-// two lanes with the probe: (lane | 0x8000) - q keeps bit 15 of its lane iff
-// lane >= q, and no borrow crosses into the other lane.
+// Compressed nodes of 16 lanes (node width 15): lane 0 = 0xFFC0 | s, lanes
+// 1..15 = 0x8000 | ((separator - B) >> s), a 14-bit delta of at most
+// kBtreeMaxDelta16; 0xFFFF past the column's end.  Lane i sits in logical
+// word i / 2, low half for even i.  With every lane in [0x8000, 0xFFFF] and
+// the probe value kd at most 0x3FFE, one 32-bit subtraction compares two
+// lanes with the probe: lane - kd stays in [0x4002, 0xFFFF], so no borrow
+// crosses into the other lane, and bit 15 of a separator lane is set iff its
+// delta >= kd.  The header and absent lanes always count as >= kd.
 constexpr uint32_t kBtreeCompressed16 = 15;
-constexpr uint32_t kBtreeAbsent16 = 0x7FFFu;
-constexpr uint32_t kBtreeMaxDelta16 = 0x7FFEu;
+constexpr uint32_t kBtreeAbsent16 = 0xFFFFu;
+constexpr uint32_t kBtreeHeader16 = 0xFFC0u;
+constexpr uint32_t kBtreeLaneBias16 = 0x8000u;
+constexpr uint32_t kBtreeMaxDelta16 = 0x3FFEu;
 
+// delta of lane i (bias removed)
 GJ_DEVICE_INLINE uint32_t lane16(const uint32_t (&w)[8], uint32_t i) {
-    const uint32_t x = pick8(w, i >> 1);
-    return (i & 1) ? x >> 16 : x & 0xFFFFu;
+    return __byte_perm(pick8(w, i >> 1), 0, (i & 1) ? 0x4432u : 0x4410u) & 0x7FFFu;
 }
 
 template <int kInner, bool kExact>
@@ -309,10 +313,10 @@ GJ_DEVICE_INLINE uint32_t btree_c15_child(const btree_view& v, const uint32_t (&
     const uint64_t q = (key - *B) >> sh;
     const uint32_t kd = q < kBtreeMaxDelta16 ? (uint32_t)q : kBtreeMaxDelta16;
     const uint32_t q2 = kd * 0x00010001u;
-    uint32_t ge = 0;  // separators >= kd
+    uint32_t ge = 0;  // lanes >= kd (the header lane always)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) ge += __popc(((w[i] | 0x80008000u) - q2) & (i == 0 ? 0x80000000u : 0x80008000u));
-    uint32_t c = 15u - ge;
+    for (int i = 0; i < 8; ++i) ge += __popc((w[i] - q2) & 0x80008000u);
+    uint32_t c = 16u - ge;
     if constexpr (kExact) {
         // separators equal to kd follow c (they are sorted): step right over
         // those whose exact key is below the probe
@@ -460,6 +464,7 @@ GJ_DEVICE_INLINE uint32_t btree_lookup_from(const btree_view& v, const uint64_t*
     bool eq;
     uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
     if constexpr (kCompressed) {
+        // a wrong left turn: search again, open slots resolved exactly
         if (pos == end && end < v.n) {  // a wrong left turn: search again, open slots resolved exactly
             j = btree_cx_descend<W, kInner, true>(v, cache, key, (int)v.height, 0u, v.min_key);
             base = j * v.leaf_keys;
@@ -512,6 +517,53 @@ GJ_DEVICE_INLINE btree_cursor btree_common_node(const btree_view& v, const uint6
         }
     }
     return c;
+}
+
+// ---------------------------------------------------------------------------
+// Linear-probing hash table: the build side of the reference's hash join
+// (src/linear_probing_hashtable.cuh:13-73, src/generic_hj.cu:7-50), kept as
+// an index kind so that every probe operator can run against it.
+// ---------------------------------------------------------------------------
+// Slots of 16 bytes (key, position, pad); the capacity is a power of two of
+// at least twice the key count (load factor <= 0.5, as the reference's
+// max_load_factor).  A slot whose position is 0xFFFFFFFF is empty: positions
+// are below n < 2^32 - 1, so every 64-bit key can be stored, UINT64_MAX (the
+// reference's empty key marker) included.  The home slot of a key is
+// MurmurHash3's 64-bit finaliser of the key (the reference hashes with
+// murmur3 as well), masked to the capacity; collisions step to the next slot.
+struct hash_slot {
+    uint64_t key;
+    uint32_t pos;
+    uint32_t pad;
+};
+struct hash_view {
+    const hash_slot* slots;
+    uint64_t mask;  // capacity - 1
+    uint64_t n;
+};
+constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+
+// fmix64 of MurmurHash3 (Austin Appleby, public domain)
+__host__ __device__ __forceinline__ uint64_t murmur3_fmix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// position of the slot holding key, else kInvalid; the table always has an
+// empty slot, and the walk is bounded by the capacity besides
+GJ_DEVICE_INLINE uint32_t hash_lookup(const hash_view& v, uint64_t key) {
+    uint64_t h = murmur3_fmix64(key) & v.mask;
+    for (uint64_t step = 0; step <= v.mask; ++step) {
+        const ulonglong2 s = __ldg(reinterpret_cast<const ulonglong2*>(v.slots + h));
+        if ((uint32_t)s.y == kHashEmpty) return kInvalid;
+        if (s.x == key) return (uint32_t)s.y;
+        h = (h + 1) & v.mask;
+    }
+    return kInvalid;
 }
 
 // ---------------------------------------------------------------------------

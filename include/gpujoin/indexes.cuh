@@ -226,6 +226,27 @@ struct learned_index : public gj::detail::index_base<GJ_INDEX_LEARNED, gj::learn
     }
 };
 
+// the reference's hash-join table (src/linear_probing_hashtable.cuh) with the
+// index interface: position of the equal key, else invalid_tid
+template <class Key, class Value, template <class T> class DeviceAllocator = std::allocator,
+          template <class T> class HostAllocator = std::allocator>
+struct hash_index : public gj::detail::index_base<GJ_INDEX_HASH, gj::hash_view, Key> {
+    using key_t = Key;
+    using value_t = Value;
+    static constexpr value_t invalid_tid = std::numeric_limits<value_t>::max();
+
+    struct device_index_t {
+        gj::hash_view v;
+        __device__ __forceinline__ value_t cooperative_lookup(const bool active, const key_t key) const {
+            return active ? gj::detail::to_tid<value_t>(gj::hash_lookup(v, key)) : invalid_tid;
+        }
+    } device_index;
+
+    void construct(const vector_view<key_t>& h_column, const key_t* d_column) override {
+        this->build(h_column, d_column, &device_index.v);
+    }
+};
+
 template <class Key, class Value, template <class T> class DeviceAllocator = std::allocator,
           template <class T> class HostAllocator = std::allocator>
 struct no_op_index : public abstract_index<Key> {

@@ -43,7 +43,7 @@ def test_abi_version_and_names(gj):
 
 def test_parse_index_type(gj):
     # src/indexes.cpp:5-19
-    for name in ("btree", "harmonia", "binary_search", "radix_spline", "no_op", "learned"):
+    for name in ("btree", "harmonia", "binary_search", "radix_spline", "no_op", "learned", "hash"):
         assert gj.parse_index_type(name).name == name
     with pytest.raises(RuntimeError, match="unknown index type"):
         gj.parse_index_type("hash_table")

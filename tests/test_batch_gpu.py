@@ -13,7 +13,7 @@ def test_batch_modes_match_oracle(orc, gj, cuda):
 
     rng = np.random.default_rng(1)
     specs = [("btree", 1 << 16, 0), ("harmonia", 1 << 15, 1), ("radix_spline", 1 << 17, 0),
-             ("binary_search", 1 << 14, 2), ("learned", 1 << 16, 1)]
+             ("binary_search", 1 << 14, 2), ("learned", 1 << 16, 1), ("hash", 1 << 16, 2)]
     indexes, cols = [], []
     for i, (kind, n, dist) in enumerate(specs):
         keys = gj.generate_sorted_keys(n, dist, 1 << 63, seed=100 + i)
@@ -37,7 +37,7 @@ def test_batch_modes_match_oracle(orc, gj, cuda):
         a, e = int(offs[b]), int(offs[b]) + int(sizes[b])
         col = cols[which[b]].cpu().numpy().view(np.uint64)
         kind = specs[which[b]][0]
-        exp[a:e] = (orc.exact_lookup if kind in ("btree", "harmonia") else orc.bs_lookup)(col, h_probes[a:e])
+        exp[a:e] = (orc.exact_lookup if kind in ("btree", "harmonia", "hash") else orc.bs_lookup)(col, h_probes[a:e])
     for mode in (0, 1):
         out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
         done = torch.zeros(nb + 1, dtype=torch.int64, device="cuda")

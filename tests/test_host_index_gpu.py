@@ -52,6 +52,21 @@ def test_host_btree_pairs_and_partitioned(orc, gj, cuda, node_keys, leaf_keys):
     np.testing.assert_array_equal(pos[order], epos)
 
 
+@pytest.mark.parametrize("kind", ["btree", "radix_spline", "learned"])
+def test_host_column_device_index(orc, gj, cuda, kind):
+    # column in Grace memory, the index's own arrays (inner levels, spline,
+    # models) in HBM
+    import torch
+
+    rng = np.random.default_rng(41)
+    col = column(rng, 1 << 17)
+    pr = probes_for(rng, col, 1 << 16)
+    ix = gj.make_index(kind).construct(None, host_column(torch, col))
+    assert ix.host_memory() == 0
+    got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+    np.testing.assert_array_equal(got, expected(orc, kind, col, pr))
+
+
 def test_device_index_has_no_host_arrays(gj, cuda):
     import torch
 
@@ -69,4 +84,4 @@ def test_host_index_rejects_bad_placement(gj, cuda):
     with pytest.raises(gj.GJError):
         gj.btree_index(index_memory=7).construct(None, to_dev(torch, col))
     with pytest.raises(ValueError):
-        gj.btree_index().construct(None, host_column(torch, col))  # a host column needs a host-memory index
+        gj.btree_index().construct(None, torch.from_numpy(col.view(np.int64)))  # pageable host memory

@@ -14,7 +14,7 @@ def pairs_of(out_pairs, count):
     return a[:, 0].copy(), a[:, 1].copy()
 
 
-@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline"])
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline", "hash"])
 @pytest.mark.parametrize("m", [0, 1, 31, 2047, 2048, 2049, 100003])
 def test_inlj_pairs_match_oracle(orc, gj, cuda, kind, m):
     import torch
@@ -127,7 +127,7 @@ def test_partitioned_inlj_fanouts(orc, gj, cuda, bits):
     np.testing.assert_array_equal(bpos[order], epos)
 
 
-@pytest.mark.parametrize("kind", ["btree", "harmonia", "radix_spline", "binary_search", "learned"])
+@pytest.mark.parametrize("kind", ["btree", "harmonia", "radix_spline", "binary_search", "learned", "hash"])
 def test_partitioned_pairs_sorted_tiles(orc, gj, cuda, kind):
     # tiles of equal keys, a tile spanning the whole key range, many windows
     import torch

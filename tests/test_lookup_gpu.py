@@ -44,7 +44,7 @@ def expected(orc, kind, col, pr):
     return orc.exact_lookup(col, pr)
 
 
-@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline"])
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline", "hash"])
 @pytest.mark.parametrize("n", [32, 64, 96, 2048, 32 * 1090, 100000 - 100000 % 32, 1 << 20])
 def test_lookup_matches_oracle(orc, gj, cuda, kind, n):
     import torch
@@ -60,7 +60,7 @@ def test_lookup_matches_oracle(orc, gj, cuda, kind, n):
     assert len(bad) == 0, f"{kind} n={n}: {len(bad)} mismatches, first {bad[:5]} got {got[bad[:5]]} exp {exp[bad[:5]]}"
 
 
-@pytest.mark.parametrize("kind", ["binary_search", "btree", "radix_spline"])
+@pytest.mark.parametrize("kind", ["binary_search", "btree", "radix_spline", "hash"])
 @pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 63, 65, 4095, 4097])
 def test_lookup_small_ragged_sizes(orc, gj, cuda, kind, n):
     import torch
@@ -262,3 +262,22 @@ def test_lookup_on_side_stream(orc, gj, cuda):
         out = ix.lookup(d_pr, stream=s)
     s.synchronize()
     np.testing.assert_array_equal(from_dev_u32(out), orc.exact_lookup(col, pr))
+
+
+def test_hash_index_edge_keys(orc, gj, cuda):
+    # keys at both ends of the 64-bit range (UINT64_MAX is storable: empty
+    # slots are marked in the position word), dense runs that collide in the
+    # table's low bits, and probes on every key and both neighbours
+    import torch
+
+    rng = np.random.default_rng(77)
+    for name, col in compressed_key_sets(rng).items():
+        col = np.ascontiguousarray(col, dtype=np.uint64)
+        if name == "near_top":
+            assert col[-1] == np.uint64((1 << 64) - 1)
+        pr = np.concatenate([col, col - np.uint64(1), col + np.uint64(1),
+                             np.array([0, 1, (1 << 64) - 1, 1 << 63], dtype=np.uint64)])
+        ix = gj.hash_index().construct(None, to_dev(torch, col))
+        assert ix.memory_consumption() >= 16 * 2 * len(col)
+        got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=name)
