@@ -231,7 +231,8 @@ def gpu_setup():
 def gpu_main(args):
     world, rank, device, stream = gpu_setup()
     fn = {"inlj": inlj_workload, "partitioned": partitioned_workload, "star": star_workload,
-          "learned": learned_workload, "batch": batch_workload, "host_index": host_index_workload}[args.workload]
+          "learned": learned_workload, "batch": batch_workload, "host_index": host_index_workload,
+          "orderings": orderings_workload}[args.workload]
     line = fn(args, world, rank, device, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -571,6 +572,52 @@ def host_index_workload(args, world, rank, device, stream):
          "gpu_launches": 2 * args.steps, "cpu_baseline": None, "e2e": None})
 
 
+def orderings_workload(args, world, rank, device, stream):
+    """Probe order as an autotuner choice (the reference's block-wise sorted
+    lookups, src/index_lookup_common.cuh:398-549): INLJ pairs of 2^m_log2
+    probes into 2^n_log2 keys in probe order and from sorted tiles, over
+    Zipf theta 0 (uniform), 0.5 and 1.0, with the autotuner's pick."""
+    import ctypes
+
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    n, m = 1 << args.n_log2, 1 << args.m_log2
+    kind = args.indexes.split(",")[0]
+    keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
+    ix = gj.make_index(kind, **index_params(args, kind)).construct(None, keys)
+    pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device)
+    wsz = ctypes.c_size_t(0)
+    gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(wsz))
+    ws = torch.empty(wsz.value, dtype=torch.uint8, device=device)
+    thetas, head = {}, None
+    for theta in (0.0, 0.5, 1.0):
+        probes = gj.generate_probes(keys, m, theta=theta, seed=args.seed + 1)
+        row = {}
+        for name, fn in (("probe", ix.inlj_pairs), ("sorted_tiles", ix.inlj_pairs_sorted)):
+            ms = time_steps(lambda: fn(probes, pairs, count, ws), args.steps, args.warmup, stream, world, device)
+            ms = max_over_ranks(ms, world, device)
+            row[name] = {"tuples_per_s": world * m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                         "pairs": int(count.item())}
+        pick, _ = ix.autotune_ordering(probes)
+        row["autotune"] = "sorted_tiles" if pick == gj.ORDER_SORTED_TILES else "probe"
+        row["same_pairs"] = row["probe"]["pairs"] == row["sorted_tiles"]["pairs"]
+        thetas[str(theta)] = row
+        if theta == args.theta:
+            head = row
+        del probes
+    head = head or thetas["0.5"]
+    best = head[head["autotune"]]
+    return _base_line(
+        args, world, f"INLJ probe tuples/s ({kind}, autotuned probe order, 1 GB300 per rank)", best["tuples_per_s"],
+        "probe tuples/s", best["ms_per_step"],
+        f"INLJ pairs: {n} uniform uint64 build keys, {m} Zipf probes (theta 0, 0.5, 1.0), probe order vs "
+        f"block-wise sorted tiles of 1024",
+        {"orderings": {"index": kind, "thetas": thetas}, "gpu_launches": None, "cpu_baseline": None, "e2e": None})
+
+
 def star_inputs(n_fact, n_dim, seed, device):
     import torch
 
@@ -814,8 +861,8 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch", "host_index"],
-                    default="inlj")
+    ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch", "host_index",
+                                           "orderings"], default="inlj")
     ap.add_argument("--host-n-log2", default="26,28", help="host_index: column sizes (log2 keys)")
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)

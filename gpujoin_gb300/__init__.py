@@ -85,6 +85,10 @@ class gj_index_params(ctypes.Structure):
     ]
 
 
+# probe orders (gj_autotune_ordering)
+ORDER_PROBE = 0
+ORDER_SORTED_TILES = 1
+
 # gj_index_params.index_memory
 INDEX_MEMORY_DEVICE = 0
 INDEX_MEMORY_HOST = 1
@@ -127,6 +131,9 @@ _SIGNATURES = {
     "gj_learned_mlp_grad": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_autotune_partitioned": (_i32, [_vp, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u64),
                                        ctypes.POINTER(ctypes.c_float)]),
+    "gj_index_lookup_sorted": (_i32, [_vp, _vp, _u64, _vp, _vp]),
+    "gj_inlj_pairs_sorted": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_autotune_ordering": (_i32, [_vp, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(ctypes.c_float)]),
     "gj_autotune_btree": (_i32, [_vp, _u64, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
                                  ctypes.POINTER(ctypes.c_float)]),
     "gj_autotune_partitioned_btree": (_i32, [_vp, _u64, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
@@ -319,6 +326,39 @@ class abstract_index:
         _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
                                    _ptr(workspace), workspace.numel(), _stream(stream)))
         return out_pairs, out_count
+
+    def lookup_sorted(self, d_probes, out=None, stream=None):
+        """Block-wise sorted lookup (bws_lookup, src/index_lookup_common.cuh:398-549): the positions of lookup()."""
+        torch = _torch()
+        m = d_probes.numel()
+        if out is None:
+            out = _empty(m, torch.int32, d_probes.device)
+        _check(lib().gj_index_lookup_sorted(self.handle, _ptr(d_probes), m, _ptr(out), _stream(stream)))
+        return out
+
+    def inlj_pairs_sorted(self, d_probes, out_pairs=None, out_count=None, workspace=None, stream=None):
+        """The pairs of inlj_pairs() from block-wise sorted tiles (key order inside a tile)."""
+        torch = _torch()
+        m = d_probes.numel()
+        dev = d_probes.device
+        if out_pairs is None:
+            out_pairs = _empty(2 * max(m, 1), torch.int32, dev)
+        if out_count is None:
+            out_count = torch.zeros(1, dtype=torch.int64, device=dev)
+        if workspace is None:
+            need = _sz(0)
+            _check(lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(need)))
+            workspace = _workspace(need.value, dev)
+        _check(lib().gj_inlj_pairs_sorted(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
+                                          _ptr(workspace), workspace.numel(), _stream(stream)))
+        return out_pairs, out_count
+
+    def autotune_ordering(self, d_probes, stream=None):
+        """(ORDER_PROBE or ORDER_SORTED_TILES, best ms) for pairs of these probes."""
+        o, ms = _u32(0), ctypes.c_float(0)
+        _check(lib().gj_autotune_ordering(self.handle, _ptr(d_probes), d_probes.numel(), _stream(stream),
+                                          ctypes.byref(o), ctypes.byref(ms)))
+        return o.value, ms.value
 
     def inlj_pairs_host(self, h_probes, h_pairs, h_count, workspace=None, stream=None):
         """inlj_pairs on pinned HOST tensors (probes int64, pairs int32 of 2m, count int64 of 1): the

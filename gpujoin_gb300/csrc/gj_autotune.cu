@@ -146,6 +146,37 @@ int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint
     return GJ_OK;
 }
 
+int gj_autotune_ordering(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
+                         uint32_t* ordering, float* best_ms) {
+    GJ_CHECK_ARG(index && ordering, "gj_autotune_ordering: null argument");
+    GJ_CHECK_ARG(m > 0 && d_probes, "gj_autotune_ordering: no probes");
+    cudaStream_t s = as_stream(stream);
+    size_t ws_bytes = 0;
+    GJ_TRY(gj_inlj_pairs_workspace_size(m, &ws_bytes));
+    device_buffer ws, pairs, count;
+    GJ_TRY(ws.alloc(ws_bytes));
+    GJ_TRY(pairs.alloc(2 * m * sizeof(uint32_t)));
+    GJ_TRY(count.alloc(sizeof(uint64_t)));
+    event_pair ev;
+    GJ_TRY(ev.init());
+    float t_probe = 0.f, t_sorted = 0.f;
+    GJ_TRY(time_best(
+        [&] {
+            return gj_inlj_pairs(index, d_probes, m, static_cast<uint32_t*>(pairs.p), static_cast<uint64_t*>(count.p),
+                                 ws.p, ws_bytes, stream);
+        },
+        s, 2, ev, &t_probe));
+    GJ_TRY(time_best(
+        [&] {
+            return gj_inlj_pairs_sorted(index, d_probes, m, static_cast<uint32_t*>(pairs.p),
+                                        static_cast<uint64_t*>(count.p), ws.p, ws_bytes, stream);
+        },
+        s, 2, ev, &t_sorted));
+    *ordering = t_sorted < t_probe ? GJ_ORDER_SORTED_TILES : GJ_ORDER_PROBE;
+    if (best_ms) *best_ms = t_sorted < t_probe ? t_sorted : t_probe;
+    return GJ_OK;
+}
+
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms) {
     GJ_CHECK_ARG(node_keys && leaf_keys, "gj_autotune_btree: null argument");

@@ -750,6 +750,25 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
                         d_pairs ? d_pairs + m : nullptr, as_stream(stream));
 }
 
+int gj_index_lookup_sorted(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,
+                           void* stream) {
+    GJ_CHECK_ARG(index, "gj_index_lookup_sorted: null index");
+    GJ_CHECK_ARG(m == 0 || (d_probes && d_positions), "gj_index_lookup_sorted: null buffer");
+    return launch_sorted_lookup(index, d_probes, m, d_positions, as_stream(stream));
+}
+
+int gj_inlj_pairs_sorted(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                         uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(index && d_count, "gj_inlj_pairs_sorted: null argument");
+    GJ_CHECK_ARG(m == 0 || (d_probes && d_pairs), "gj_inlj_pairs_sorted: null buffer");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_inlj_pairs_sorted: probe rows must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    return launch_partitioned_pairs(index, d_probes, nullptr, m, d_pairs, nullptr, d_count, d_workspace,
+                                    workspace_bytes, as_stream(stream));
+}
+
 // device address of a caller buffer the GPU may touch: pinned or registered
 // host memory (through NVLink-C2C / PCIe), managed or device memory, or
 // pageable host memory on systems where the GPU reads the CPU's page tables

@@ -130,6 +130,7 @@ struct gj_index {
 namespace gj {
 // lookup entry points shared between translation units (gj_lookup.cu)
 int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s);
+int launch_sorted_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s);
 int launch_scatter_lookup(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
                           uint32_t* d_out, cudaStream_t s);
 // Pairs are written from offset *d_base (0 if null); *d_count = base +

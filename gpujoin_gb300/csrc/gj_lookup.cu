@@ -39,6 +39,12 @@ int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uin
                           nullptr, s});
 }
 
+int launch_sorted_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s) {
+    if (m == 0) return GJ_OK;
+    return dispatch(idx, {lookup_action::sorted_positions, d_probes, nullptr, m, d_out, nullptr, nullptr, nullptr, 0,
+                          nullptr, s});
+}
+
 int launch_scatter_lookup(const gj_index* idx, const uint64_t* d_keys, const uint32_t* d_rows, uint64_t m,
                           uint32_t* d_out, cudaStream_t s) {
     if (m == 0) return GJ_OK;

@@ -25,7 +25,7 @@
 namespace gj {
 
 // one launch of a probe kernel for an index, as passed between the units
-enum class lookup_action { positions, scatter, pairs, sorted_pairs };
+enum class lookup_action { positions, scatter, pairs, sorted_pairs, sorted_positions };
 struct lookup_call {
     lookup_action action;
     const uint64_t* keys;  // probes, or the keys of a partitioned relation
@@ -490,9 +490,125 @@ static_assert(kStateTile <= kSortTile && kStateTile <= kTile && kStateTile <= kC
 
 __device__ __forceinline__ unsigned bit_length(uint64_t v) { return v ? 64u - (unsigned)__clzll(v) : 0u; }
 
-// about 21 KB of shared memory per block; 6 resident blocks (40 registers),
-// fewer for index kinds compiled for fewer
+// Shared memory of one sorted tile (about 21 KB with the kernels' caches).
+template <class Hint>
+struct sorted_tile_smem {
+    static constexpr int kWarps = kBlock / 32;
+    uint64_t key[kSortTile];
+    uint32_t row[kSortTile];
+    __align__(16) uint32_t bucket[kSortBuckets];  // read as uint4
+    unsigned long long lo[kWarps], hi[kWarps];
+    uint32_t wsum[kWarps];
+    Hint hint;
+};
+
+// Sorts the tile keys[t0 .. t0 + tn) by key into t.key, with row_of(j) (j =
+// item inside the tile) beside each in t.row, and (for an op with a tile
+// hint) leaves the hint of the tile's key range in t.hint.  Ends with a
+// barrier.  The caller's previous reads of t must be behind a barrier.
+template <class Op, class RowOf>
+__device__ __forceinline__ void sort_tile(const Op& op, const uint64_t* cache, const uint64_t* __restrict__ keys,
+                                          uint64_t t0, uint32_t tn, RowOf&& row_of,
+                                          sorted_tile_smem<typename tile_hint_of<Op>::type>& t) {
+    constexpr int kWarps = kBlock / 32;
+    constexpr bool kHinted = !std::is_same<typename tile_hint_of<Op>::type, no_tile_hint>::value;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t key[kSortItems];
+    unsigned long long lo = ~0ull, hi = 0ull;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const uint32_t j = k * kBlock + threadIdx.x;
+        key[k] = j < tn ? __ldcs(reinterpret_cast<const unsigned long long*>(keys) + t0 + j) : 0ull;
+        if (j < tn) {
+            lo = key[k] < lo ? key[k] : lo;
+            hi = key[k] > hi ? key[k] : hi;
+        }
+    }
+    // key range of the tile
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+        const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, d);
+        const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, d);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    if (lane == 0) {
+        t.lo[warp] = lo;
+        t.hi[warp] = hi;
+    }
+    for (uint32_t b = threadIdx.x; b < kSortBuckets; b += kBlock) t.bucket[b] = 0;
+    __syncthreads();
+    lo = t.lo[0];
+    hi = t.hi[0];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) {
+        lo = t.lo[w] < lo ? t.lo[w] : lo;
+        hi = t.hi[w] > hi ? t.hi[w] : hi;
+    }
+    if constexpr (kHinted) {
+        if (threadIdx.x == 0) t.hint = op.tile(cache, lo, hi);  // read after the barriers below
+    }
+    const unsigned used = bit_length(hi - lo);
+    constexpr unsigned kBucketBits = 10;  // kSortBuckets = 2^10
+    const unsigned sh = used > kBucketBits ? used - kBucketBits : 0;  // (hi - lo) >> sh < kSortBuckets
+    // counting sort: ranks inside a bucket from shared-memory atomics
+    uint32_t rank[kSortItems];
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const uint32_t j = k * kBlock + threadIdx.x;
+        rank[k] = j < tn ? atomicAdd(&t.bucket[(uint32_t)((key[k] - lo) >> sh)], 1u) : 0u;
+    }
+    __syncthreads();
+    {
+        // exclusive scan of the buckets: kSortBuckets / kBlock consecutive per thread
+        static_assert(kSortBuckets / kBlock == 4, "one uint4 per thread");
+        uint4* sb = reinterpret_cast<uint4*>(t.bucket) + threadIdx.x;
+        const uint4 c0 = sb[0];
+        const uint32_t sum = c0.x + c0.y + c0.z + c0.w;
+        uint32_t incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += v;
+        }
+        if (lane == 31) t.wsum[warp] = incl;
+        __syncthreads();
+        uint32_t run = incl - sum;
+        for (int w = 0; w < (int)warp; ++w) run += t.wsum[w];
+        uint4 o0;
+        o0.x = run; run += c0.x;
+        o0.y = run; run += c0.y;
+        o0.z = run; run += c0.z;
+        o0.w = run;
+        sb[0] = o0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const uint32_t j = k * kBlock + threadIdx.x;
+        if (j < tn) {
+            const uint32_t q = t.bucket[(uint32_t)((key[k] - lo) >> sh)] + rank[k];
+            t.key[q] = key[k];
+            t.row[q] = row_of(j);
+        }
+    }
+    __syncthreads();
+}
+
+// item j of a sorted tile: its search, from the tile's hint when the op has one
 template <class Op>
+__device__ __forceinline__ uint32_t sorted_lookup(const Op& op, const uint64_t* cache, uint64_t key,
+                                                  const typename tile_hint_of<Op>::type& h) {
+    if constexpr (std::is_same<typename tile_hint_of<Op>::type, no_tile_hint>::value)
+        return op.template lookup<false>(cache, key);
+    else
+        return op.lookup_in_tile(cache, key, h);
+}
+
+// about 21 KB of shared memory per block; 6 resident blocks (40 registers),
+// fewer for index kinds compiled for fewer.  kRows = false: no row ids, the
+// row of probe i is i (plain probes in sorted tiles).
+template <class Op, bool kRows>
 __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 6) k_sorted_pairs(const __grid_constant__ Op op, const stage_desc sd,
                                                          const uint64_t* __restrict__ keys,
                                                          const uint32_t* __restrict__ rows, uint64_t m,
@@ -501,120 +617,67 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 
                                                          uint64_t* __restrict__ d_count, pairs_ws ws,
                                                          uint32_t num_tiles) {
     extern __shared__ __align__(16) uint64_t cache[];
-    constexpr int kWarps = kBlock / 32;
-    __shared__ uint64_t s_key[kSortTile];
-    __shared__ uint32_t s_row[kSortTile];
-    __shared__ __align__(16) uint32_t s_bucket[kSortBuckets];  // read as uint4
-    __shared__ unsigned long long s_lo[kWarps], s_hi[kWarps];
     using hint_t = typename tile_hint_of<Op>::type;
-    constexpr bool kHinted = !std::is_same<hint_t, no_tile_hint>::value;
-    __shared__ hint_t s_hint;
+    __shared__ sorted_tile_smem<hint_t> t;
     stage_cache(cache, sd);
     const uint64_t base = d_base ? *d_base : 0ull;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     auto fill = [&](uint64_t t0, uint32_t* s_pos) {
         const uint32_t tn = m - t0 < kSortTile ? (uint32_t)(m - t0) : kSortTile;
-        uint64_t key[kSortItems];
-        unsigned long long lo = ~0ull, hi = 0ull;
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            key[k] = j < tn ? __ldcs(reinterpret_cast<const unsigned long long*>(keys) + t0 + j) : 0ull;
-            if (j < tn) {
-                lo = key[k] < lo ? key[k] : lo;
-                hi = key[k] > hi ? key[k] : hi;
-            }
-        }
-        // key range of the tile
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) {
-            const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, d);
-            const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, d);
-            lo = a < lo ? a : lo;
-            hi = b > hi ? b : hi;
-        }
-        if (lane == 0) {
-            s_lo[warp] = lo;
-            s_hi[warp] = hi;
-        }
-        for (uint32_t b = threadIdx.x; b < kSortBuckets; b += kBlock) s_bucket[b] = 0;
-        __syncthreads();
-        lo = s_lo[0];
-        hi = s_hi[0];
-#pragma unroll
-        for (int w = 1; w < kWarps; ++w) {
-            lo = s_lo[w] < lo ? s_lo[w] : lo;
-            hi = s_hi[w] > hi ? s_hi[w] : hi;
-        }
-        if constexpr (kHinted) {
-            if (threadIdx.x == 0) s_hint = op.tile(cache, lo, hi);  // read after the barriers below
-        }
-        const unsigned used = bit_length(hi - lo);
-        constexpr unsigned kBucketBits = 10;  // kSortBuckets = 2^10
-        const unsigned sh = used > kBucketBits ? used - kBucketBits : 0;  // (hi - lo) >> sh < kSortBuckets
-        // counting sort: ranks inside a bucket from shared-memory atomics
-        uint32_t rank[kSortItems];
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            rank[k] = j < tn ? atomicAdd(&s_bucket[(uint32_t)((key[k] - lo) >> sh)], 1u) : 0u;
-        }
-        __syncthreads();
-        {
-            // exclusive scan of the buckets: kSortBuckets / kBlock consecutive per thread
-            static_assert(kSortBuckets / kBlock == 4, "one uint4 per thread");
-            uint4* sb = reinterpret_cast<uint4*>(s_bucket) + threadIdx.x;
-            const uint4 c0 = sb[0];
-            const uint32_t sum = c0.x + c0.y + c0.z + c0.w;
-            uint32_t incl = sum;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= (uint32_t)d) incl += t;
-            }
-            __shared__ uint32_t s_wsum[kWarps];
-            if (lane == 31) s_wsum[warp] = incl;
-            __syncthreads();
-            uint32_t run = incl - sum;
-            for (int w = 0; w < (int)warp; ++w) run += s_wsum[w];
-            uint4 o0;
-            o0.x = run; run += c0.x;
-            o0.y = run; run += c0.y;
-            o0.z = run; run += c0.z;
-            o0.w = run;
-            sb[0] = o0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kSortItems; ++k) {
-            const uint32_t j = k * kBlock + threadIdx.x;
-            if (j < tn) {
-                const uint32_t q = s_bucket[(uint32_t)((key[k] - lo) >> sh)] + rank[k];
-                s_key[q] = key[k];
-                s_row[q] = __ldcs(rows + t0 + j);
-            }
-        }
-        __syncthreads();
-        if constexpr (kHinted) {
-            const hint_t h = s_hint;
+        sort_tile(op, cache, keys, t0, tn,
+                  [&](uint32_t j) {
+                      if constexpr (kRows) return __ldcs(rows + t0 + j);
+                      else return (uint32_t)(t0 + j);
+                  },
+                  t);
+        const hint_t h = t.hint;
 #pragma unroll 1
-            for (int k = 0; k < kSortItems; ++k) {
-                const uint32_t j = k * kBlock + threadIdx.x;
-                s_pos[j] = j < tn ? op.lookup_in_tile(cache, s_key[j], h) : kInvalid;
-            }
-        } else {
-#pragma unroll 1
-            for (int k = 0; k < kSortItems; ++k) {
-                const uint32_t j = k * kBlock + threadIdx.x;
-                s_pos[j] = j < tn ? op.template lookup<false>(cache, s_key[j]) : kInvalid;
-            }
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            s_pos[j] = j < tn ? sorted_lookup(op, cache, t.key[j], h) : kInvalid;
         }
     };
-    auto row_of = [&](int k, uint64_t) { return s_row[k * kBlock + threadIdx.x]; };
+    auto row_of = [&](int k, uint64_t) { return t.row[k * kBlock + threadIdx.x]; };
     for (;;) {
         const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
         if (!pairs_tile<kSortItems>(fill, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
+    }
+}
+
+// Block-wise sorted lookup (the reference's bws_lookup,
+// src/index_lookup_common.cuh:398-549): each tile of kSortTile probes is
+// sorted by key, searched in that order, and the positions are put back in
+// probe order through shared memory: out[i] = lookup(probes[i]).  A block
+// takes kSortedLookupTiles consecutive tiles (the shared cache is staged
+// once for them).
+constexpr uint32_t kSortedLookupTiles = 4;
+template <class Op>
+__global__ void __launch_bounds__(kBlock, Op::kMinBlocks < 6 ? Op::kMinBlocks : 6) k_sorted_lookup(const __grid_constant__ Op op, const stage_desc sd,
+                                                          const uint64_t* __restrict__ probes, uint64_t m,
+                                                          uint32_t* __restrict__ out) {
+    extern __shared__ __align__(16) uint64_t cache[];
+    using hint_t = typename tile_hint_of<Op>::type;
+    __shared__ sorted_tile_smem<hint_t> t;
+    __shared__ uint32_t s_pos[kSortTile];
+    stage_cache(cache, sd);
+    for (uint32_t r = 0; r < kSortedLookupTiles; ++r) {
+        const uint64_t t0 = ((uint64_t)blockIdx.x * kSortedLookupTiles + r) * kSortTile;
+        if (t0 >= m) break;
+        const uint32_t tn = m - t0 < kSortTile ? (uint32_t)(m - t0) : kSortTile;
+        sort_tile(op, cache, probes, t0, tn, [](uint32_t j) { return j; }, t);
+        const hint_t h = t.hint;
+#pragma unroll 1
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            if (j < tn) s_pos[t.row[j]] = sorted_lookup(op, cache, t.key[j], h);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = k * kBlock + threadIdx.x;
+            if (j < tn) __stcs(out + t0 + j, s_pos[j]);
+        }
+        __syncthreads();  // t and s_pos are reused by the next tile
     }
 }
 
@@ -697,6 +760,18 @@ int run_lookup(const Op& op, const stage_desc& sd, const uint64_t* probes, uint6
 }
 
 template <class Op>
+int run_sorted_lookup(const Op& op, const stage_desc& sd, const uint64_t* probes, uint64_t m, uint32_t* out,
+                      cudaStream_t s) {
+    const size_t smem = stage_bytes(sd);
+    GJ_TRY(prepare_smem(k_sorted_lookup<Op>, smem));
+    const uint64_t per_block = (uint64_t)kSortTile * kSortedLookupTiles;
+    const uint64_t grid = (m + per_block - 1) / per_block;
+    k_sorted_lookup<Op><<<(unsigned)grid, kBlock, smem, s>>>(op, sd, probes, m, out);
+    GJ_CUDA_TRY(cudaGetLastError());
+    return GJ_OK;
+}
+
+template <class Op>
 int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const uint32_t* rows, uint64_t m,
                 uint32_t* out, cudaStream_t s) {
     const size_t smem = stage_bytes(sd);
@@ -768,9 +843,15 @@ int run_sorted_pairs(const Op& op, const stage_desc& sd, const uint64_t* keys, c
     GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
     const size_t smem = stage_bytes(sd);
     int grid = 0;
-    GJ_TRY(grid_for(k_sorted_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));
-    k_sorted_pairs<Op><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, reinterpret_cast<uint2*>(pairs), d_base,
-                                                  d_count, pw, num_tiles);
+    if (rows) {
+        GJ_TRY(grid_for(k_sorted_pairs<Op, true>, smem, (uint64_t)num_tiles * kBlock, &grid));
+        k_sorted_pairs<Op, true><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, reinterpret_cast<uint2*>(pairs),
+                                                            d_base, d_count, pw, num_tiles);
+    } else {
+        GJ_TRY(grid_for(k_sorted_pairs<Op, false>, smem, (uint64_t)num_tiles * kBlock, &grid));
+        k_sorted_pairs<Op, false><<<grid, kBlock, smem, s>>>(op, sd, keys, rows, m, reinterpret_cast<uint2*>(pairs),
+                                                             d_base, d_count, pw, num_tiles);
+    }
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
 }
@@ -785,6 +866,7 @@ int run_call(const Op& op, const gj_index* idx, const lookup_call& c) {
             return run_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.stash, c.s);
         case lookup_action::sorted_pairs:
             return run_sorted_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.s);
+        case lookup_action::sorted_positions: return run_sorted_lookup(op, sd, c.keys, c.m, c.out, c.s);
     }
     set_error("probe kernels: unknown action");
     return GJ_ERR_INVALID_ARGUMENT;

@@ -162,6 +162,23 @@ int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ---- block-wise sorted probe order ---------------------------------------- */
+/* bws_lookup (src/index_lookup_common.cuh:398-549): each tile of 1024 probes
+ * is sorted by key in shared memory and searched in that order, so lanes of
+ * a warp share index paths (skewed probes repeat keys).
+ * gj_index_lookup_sorted: the positions of gj_index_lookup, in probe order.
+ * gj_inlj_pairs_sorted: the pairs of gj_inlj_pairs, tile by tile in probe
+ * order, inside a tile in key order (the same set).  Same workspace. */
+int gj_index_lookup_sorted(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,
+                           void* stream);
+int gj_inlj_pairs_sorted(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                         uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
+#define GJ_ORDER_PROBE 0u        /* gj_inlj_pairs */
+#define GJ_ORDER_SORTED_TILES 1u /* gj_inlj_pairs_sorted */
+/* the faster probe order for these probes (pairs), timed on the caller's data */
+int gj_autotune_ordering(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
+                         uint32_t* ordering, float* best_ms);
+
 /* gj_inlj_pairs with the probes, the pairs and the count in HOST memory
  * (the reference's driver starts from host columns, src/index_lookup_new.cu:
  * 375-434).  No copies are issued: one kernel reads each tile's probes over
