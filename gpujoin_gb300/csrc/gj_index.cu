@@ -174,20 +174,22 @@ __global__ void k_hash_clear(hash_slot* slots, uint64_t capacity) {
 }
 
 // insert (src/linear_probing_hashtable.cuh:36-46): claim the first free slot
-// from the key's home slot on; the keys are unique, so no slot is matched
+// from the key's home bucket on; the keys are unique, so no slot is matched
 __global__ void k_hash_insert(const uint64_t* __restrict__ col, uint64_t n, hash_slot* slots, uint64_t mask,
                               unsigned int* full) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = col[i];
-        uint64_t h = murmur3_fmix64(key) & mask;
+        uint64_t b = murmur3_fmix64(key) & mask;
         bool placed = false;
-        for (uint64_t step = 0; step <= mask; ++step) {
-            if (atomicCAS(&slots[h].pos, kHashEmpty, (uint32_t)i) == kHashEmpty) {
-                slots[h].key = key;
-                placed = true;
-                break;
+        for (uint64_t step = 0; step <= mask && !placed; ++step) {
+            for (uint64_t s = 2 * b; s < 2 * b + 2; ++s) {
+                if (atomicCAS(&slots[s].pos, kHashEmpty, (uint32_t)i) == kHashEmpty) {
+                    slots[s].key = key;
+                    placed = true;
+                    break;
+                }
             }
-            h = (h + 1) & mask;
+            b = (b + 1) & mask;
         }
         if (!placed) atomicExch(full, 1u);
     }
@@ -470,7 +472,7 @@ int build_hash(gj_index* idx, cudaStream_t s) {
         cudaMemsetAsync(full, 0, sizeof(unsigned int), s);
         k_hash_clear<<<(int)std::min<uint64_t>((capacity + 255) / 256, 65535), 256, 0, s>>>(table, capacity);
         k_hash_insert<<<(int)std::min<uint64_t>((n + 255) / 256, 65535), 256, 0, s>>>(idx->d_col, n, table,
-                                                                                      capacity - 1, full);
+                                                                                      capacity / 2 - 1, full);
         if (host) cudaMemcpyAsync(p, table, bytes, cudaMemcpyDefault, s);
         cudaMemcpyAsync(&h_full, full, sizeof(h_full), cudaMemcpyDeviceToHost, s);
         const cudaError_t e = cudaStreamSynchronize(s);
@@ -486,7 +488,7 @@ int build_hash(gj_index* idx, cudaStream_t s) {
     if (host) cudaFree(table);
     GJ_TRY(rc);
     idx->hs.slots = static_cast<const hash_slot*>(p);
-    idx->hs.mask = capacity - 1;
+    idx->hs.mask = capacity / 2 - 1;
     idx->hs.n = n;
     idx->bytes = bytes;
     return GJ_OK;

@@ -528,9 +528,11 @@ GJ_DEVICE_INLINE btree_cursor btree_common_node(const btree_view& v, const uint6
 // at least twice the key count (load factor <= 0.5, as the reference's
 // max_load_factor).  A slot whose position is 0xFFFFFFFF is empty: positions
 // are below n < 2^32 - 1, so every 64-bit key can be stored, UINT64_MAX (the
-// reference's empty key marker) included.  The home slot of a key is
-// MurmurHash3's 64-bit finaliser of the key (the reference hashes with
-// murmur3 as well), masked to the capacity; collisions step to the next slot.
+// reference's empty key marker) included.  The home of a key is MurmurHash3's
+// 64-bit finaliser of the key (the reference hashes with murmur3 as well).
+// Linear probing runs over buckets of two slots -- one 32-byte sector, read
+// with one load: a key goes to the first free slot of its home bucket, then
+// of the next bucket, and so on (the reference probes slot by slot).
 struct hash_slot {
     uint64_t key;
     uint32_t pos;
@@ -538,7 +540,7 @@ struct hash_slot {
 };
 struct hash_view {
     const hash_slot* slots;
-    uint64_t mask;  // capacity - 1
+    uint64_t mask;  // buckets - 1 (a bucket = 2 slots)
     uint64_t n;
 };
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
@@ -554,14 +556,18 @@ __host__ __device__ __forceinline__ uint64_t murmur3_fmix64(uint64_t k) {
 }
 
 // position of the slot holding key, else kInvalid; the table always has an
-// empty slot, and the walk is bounded by the capacity besides
+// empty slot, and the walk is bounded by the bucket count besides
 GJ_DEVICE_INLINE uint32_t hash_lookup(const hash_view& v, uint64_t key) {
-    uint64_t h = murmur3_fmix64(key) & v.mask;
+    uint64_t b = murmur3_fmix64(key) & v.mask;
     for (uint64_t step = 0; step <= v.mask; ++step) {
-        const ulonglong2 s = __ldg(reinterpret_cast<const ulonglong2*>(v.slots + h));
-        if ((uint32_t)s.y == kHashEmpty) return kInvalid;
-        if (s.x == key) return (uint32_t)s.y;
-        h = (h + 1) & v.mask;
+        uint64_t w[4];  // slot 0: key, pos | pad << 32; slot 1: key, pos | pad << 32
+        ld_sector(reinterpret_cast<const uint64_t*>(v.slots + 2 * b), w);
+        const uint32_t p0 = (uint32_t)w[1], p1 = (uint32_t)w[3];
+        if (p0 == kHashEmpty) return kInvalid;
+        if (w[0] == key) return p0;
+        if (p1 == kHashEmpty) return kInvalid;
+        if (w[2] == key) return p1;
+        b = (b + 1) & v.mask;
     }
     return kInvalid;
 }
