@@ -462,7 +462,18 @@ GJ_DEVICE_INLINE uint32_t btree_lookup_from(const btree_view& v, const uint64_t*
     uint64_t base = j * v.leaf_keys;
     uint64_t end = base + v.leaf_keys < v.n ? base + v.leaf_keys : v.n;
     bool eq;
-    uint64_t pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    uint64_t pos;
+    if (v.leaf_keys == 4 && v.col_aligned && end == base + 4) {
+        // a full leaf of one aligned sector: one load, four compares
+        uint64_t k[4];
+        ld_sector_c<kColumn>(v.col + base, k);
+        const uint32_t below = (k[0] < key ? 1u : 0u) + (k[1] < key ? 1u : 0u) + (k[2] < key ? 1u : 0u) +
+                               (k[3] < key ? 1u : 0u);
+        pos = base + below;
+        eq = below < 4 && pick4(k, below & 3u) == key;
+    } else {
+        pos = lower_bound_sectors<kColumn>(v.col, v.n, base, end, key, v.col_aligned, &eq);
+    }
     if constexpr (kCompressed) {
         // a wrong left turn: search again, open slots resolved exactly
         if (pos == end && end < v.n) {  // a wrong left turn: search again, open slots resolved exactly
