@@ -47,10 +47,20 @@ GJ_DEVICE_INLINE void ld_sector(const uint64_t* p, uint64_t (&k)[4]) {
         : "l"(p));
 }
 
+// one 32-byte sector, asking L2 to fill 64 bytes on a miss: a random sector
+// read otherwise fills 128 bytes (measured: 122.5 against 62.6 bytes of DRAM
+// reads per random load); for data without spatial locality
+GJ_DEVICE_INLINE void ld_sector_64(const uint64_t* p, uint64_t (&k)[4]) {
+    asm("ld.global.nc.L2::64B.v4.u64 {%0, %1, %2, %3}, [%4];"
+        : "=l"(k[0]), "=l"(k[1]), "=l"(k[2]), "=l"(k[3])
+        : "l"(p));
+}
+
 // L2 eviction classes for the two kinds of index data: the inner levels of a
 // tree (tens of MB, read by every probe) are kept over the column sectors a
 // probe reads once (hundreds of MB, random).  Loads carry an L2 cache policy;
-// no device-wide setting is involved.
+// no device-wide setting is involved.  Both classes serve scattered probes,
+// whose neighbouring sectors are of no use: their misses fill 64 bytes.
 enum l2_class : int { kL2Default = 0, kL2Keep = 1, kL2Stream = 2 };
 
 template <int kClass>
@@ -68,7 +78,7 @@ GJ_DEVICE_INLINE void ld_sector_c(const uint64_t* p, uint64_t (&k)[4]) {
     if constexpr (kClass == kL2Default) {
         ld_sector(p, k);
     } else {
-        asm("ld.global.nc.L2::cache_hint.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
+        asm("ld.global.nc.L2::cache_hint.L2::64B.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
             : "=l"(k[0]), "=l"(k[1]), "=l"(k[2]), "=l"(k[3])
             : "l"(p), "l"(l2_policy<kClass>()));
     }
@@ -80,7 +90,7 @@ GJ_DEVICE_INLINE uint64_t ld_ro_c(const uint64_t* p) {
         return ld_ro(p);
     } else {
         uint64_t v;
-        asm("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(l2_policy<kClass>()));
+        asm("ld.global.nc.L2::cache_hint.L2::64B.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(l2_policy<kClass>()));
         return v;
     }
 }
@@ -572,7 +582,7 @@ GJ_DEVICE_INLINE uint32_t hash_lookup(const hash_view& v, uint64_t key) {
     uint64_t b = murmur3_fmix64(key) & v.mask;
     for (uint64_t step = 0; step <= v.mask; ++step) {
         uint64_t w[4];  // slot 0: key, pos | pad << 32; slot 1: key, pos | pad << 32
-        ld_sector(reinterpret_cast<const uint64_t*>(v.slots + 2 * b), w);
+        ld_sector_64(reinterpret_cast<const uint64_t*>(v.slots + 2 * b), w);
         const uint32_t p0 = (uint32_t)w[1], p1 = (uint32_t)w[3];
         if (p0 == kHashEmpty) return kInvalid;
         if (w[0] == key) return p0;
