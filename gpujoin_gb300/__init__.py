@@ -94,6 +94,19 @@ INDEX_MEMORY_DEVICE = 0
 INDEX_MEMORY_HOST = 1
 
 
+class gj_q14_tables(ctypes.Structure):
+    _fields_ = [
+        ("n_lineitem", ctypes.c_uint64),
+        ("n_part", ctypes.c_uint64),
+        ("l_partkey", ctypes.POINTER(ctypes.c_uint32)),
+        ("l_shipdate", ctypes.POINTER(ctypes.c_uint32)),
+        ("l_extendedprice", ctypes.POINTER(ctypes.c_int64)),
+        ("l_discount", ctypes.POINTER(ctypes.c_int64)),
+        ("p_partkey", ctypes.POINTER(ctypes.c_uint64)),
+        ("p_promo", ctypes.POINTER(ctypes.c_uint8)),
+    ]
+
+
 _LIB: Optional[ctypes.CDLL] = None
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64
@@ -127,6 +140,11 @@ _SIGNATURES = {
     "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
     "gj_partitioned_inlj_workspace_size": (_i32, [_vp, _u64, _u32, ctypes.POINTER(_sz)]),
     "gj_partitioned_inlj": (_i32, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "gj_tpch_load_q14": (_i32, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(gj_q14_tables)]),
+    "gj_tpch_free_q14": (None, [ctypes.POINTER(gj_q14_tables)]),
+    "gj_tpch_day": (_i32, [_i32, _i32, _i32, ctypes.POINTER(_u32)]),
+    "gj_tpch_q14": (_i32, [ctypes.POINTER(gj_q14_tables), _vp, ctypes.POINTER(ctypes.c_int64),
+                           ctypes.POINTER(ctypes.c_double)]),
     "gj_star_join_sum": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
     "gj_learned_mlp_grad": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_autotune_partitioned": (_i32, [_vp, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u64),
@@ -533,6 +551,49 @@ def range_partition(d_keys, min_key: int, shift: int, radix_bits: int, workspace
 # --------------------------------------------------------------------------
 # star join (src/tpch/tpch_14_ij.cu, src/tpch/cpu_only.cpp:230-275)
 # --------------------------------------------------------------------------
+# --------------------------------------------------------------------------
+# TPC-H Q14 from dbgen .tbl files (src/tpch/common.cpp, src/tpch/cpu_only.cpp)
+# --------------------------------------------------------------------------
+def tpch_day(year: int, month: int, day: int) -> int:
+    """The loader's day number of a date (days since 1970-01-01)."""
+    out = _u32(0)
+    _check(lib().gj_tpch_day(year, month, day, ctypes.byref(out)))
+    return out.value
+
+
+def tpch_load_q14(lineitem_tbl: str, part_tbl: str) -> dict:
+    """Q14's columns of two .tbl files as numpy arrays (copied out of the library's buffers)."""
+    import numpy as np
+
+    t = gj_q14_tables()
+    _check(lib().gj_tpch_load_q14(lineitem_tbl.encode(), part_tbl.encode(), ctypes.byref(t)))
+    try:
+        nl, npart = int(t.n_lineitem), int(t.n_part)
+
+        def arr(ptr, n, dtype):
+            return np.ctypeslib.as_array(ptr, shape=(max(n, 1),))[:n].astype(dtype, copy=True)
+
+        return {"l_partkey": arr(t.l_partkey, nl, np.uint32), "l_shipdate": arr(t.l_shipdate, nl, np.uint32),
+                "l_extendedprice": arr(t.l_extendedprice, nl, np.int64),
+                "l_discount": arr(t.l_discount, nl, np.int64), "p_partkey": arr(t.p_partkey, npart, np.uint64),
+                "p_promo": arr(t.p_promo, npart, np.uint8)}
+    finally:
+        lib().gj_tpch_free_q14(ctypes.byref(t))
+
+
+def tpch_q14(lineitem_tbl: str, part_tbl: str, stream=None):
+    """Q14 on the GPU from two .tbl files: ((promo sum, total sum), promo_revenue percent)."""
+    t = gj_q14_tables()
+    _check(lib().gj_tpch_load_q14(lineitem_tbl.encode(), part_tbl.encode(), ctypes.byref(t)))
+    try:
+        sums = (ctypes.c_int64 * 2)()
+        rev = ctypes.c_double(0)
+        _check(lib().gj_tpch_q14(ctypes.byref(t), _stream(stream), sums, ctypes.byref(rev)))
+        return (int(sums[0]), int(sums[1])), rev.value
+    finally:
+        lib().gj_tpch_free_q14(ctypes.byref(t))
+
+
 def star_join_sum(dim_index: abstract_index, d_fk, d_date, d_price, d_discount, d_dim_flag, lo: int, hi: int,
                   out=None, stream=None):
     """Returns a 2-element int64 tensor [sum over flagged rows, sum over all rows]."""

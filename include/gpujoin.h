@@ -260,6 +260,35 @@ int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk, const uint
                      const int64_t* d_price, const int64_t* d_discount, uint64_t nfact,
                      const uint8_t* d_dim_flag, uint32_t lo, uint32_t hi, int64_t* d_out, void* stream);
 
+/* ---- TPC-H Q14 from dbgen .tbl files -------------------------------------- */
+/* The columns of Q14 (load_tables_with_aria_parser, src/tpch/common.cpp:
+ * 82-220), parsed on the host (all threads) into malloc'ed arrays:
+ * lineitem l_partkey, l_shipdate (days since 1970-01-01), l_extendedprice
+ * and l_discount (decimals x 100); part p_partkey (strictly increasing, as
+ * dbgen writes them; else GJ_ERR_UNSORTED) and p_promo (p_type LIKE
+ * 'PROMO%').  Malformed rows: GJ_ERR_INVALID_ARGUMENT naming the row.
+ * Release with gj_tpch_free_q14. */
+typedef struct gj_q14_tables {
+    uint64_t n_lineitem, n_part;
+    uint32_t* l_partkey;
+    uint32_t* l_shipdate;
+    int64_t* l_extendedprice;
+    int64_t* l_discount;
+    uint64_t* p_partkey;
+    uint8_t* p_promo;
+} gj_q14_tables;
+int gj_tpch_load_q14(const char* lineitem_tbl, const char* part_tbl, gj_q14_tables* out);
+void gj_tpch_free_q14(gj_q14_tables* tables);
+/* the loader's day number of a date (days since 1970-01-01) */
+int gj_tpch_day(int year, int month, int day, uint32_t* out_day);
+/* Q14 (query_14_part_build, src/tpch/cpu_only.cpp:230-275) on the GPU: the
+ * columns are copied to HBM, a B+tree is built over p_partkey and the star
+ * join sums summand = price * (100 - discount) over lineitems shipped in
+ * [1995-09-01, 1995-10-01) with a matching part: sums[0] over PROMO parts,
+ * sums[1] over all; *promo_revenue = 100 * sums[0] / sums[1] (0 when
+ * sums[1] is 0).  Synchronous on the stream. */
+int gj_tpch_q14(const gj_q14_tables* tables, void* stream, int64_t sums[2], double* promo_revenue);
+
 /* ---- learned position model ---------------------------------------------- */
 /* The root MLP's backward pass as the learned index's trainer runs it:
  * d_grad (same layout as d_params: W1[H] b1[H] W2[HxH, out-major] b2[H]
