@@ -119,7 +119,7 @@ int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint
     // node formats for probes that arrive grouped by key range: the plain
     // lookup's best (compressed nodes) lengthens each level's dependent chain,
     // which the partitioned kernel, with fewer warps, hides less well
-    const uint32_t formats[][2] = {{4, 8}, {4, 16}, {kBtreeCompressed, 4}, {kBtreeCompressed16, 4}};
+    const uint32_t formats[][2] = {{4, 4}, {4, 8}, {4, 16}, {kBtreeCompressed, 4}, {kBtreeCompressed16, 4}};
     float best = -1.f;
     for (const auto& f : formats) {
         gj_index_params p;

@@ -349,7 +349,7 @@ int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uin
                             uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms);
-/* B+tree node format (node x leaf width: 4 x 8, 4 x 16, 7 x 4, 15 x 4) together
+/* B+tree node format (node x leaf width: 4 x 4, 4 x 8, 4 x 16, 7 x 4, 15 x 4) together
  * with partition fanout and window for the partitioned INLJ of these probes:
  * gj_autotune_partitioned on a B+tree of each format. */
 int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m,
