@@ -1,5 +1,7 @@
 """Join materialisation, partitioned INLJ and the star-join aggregate on the
 GPU against the CPU oracle."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -212,5 +214,32 @@ def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m):
     c = int(h_cnt[0])
     got = h_pairs[: 2 * c].numpy().view(np.uint32).reshape(-1, 2)
     erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
+    np.testing.assert_array_equal(got[:, 0], erows)
+    np.testing.assert_array_equal(got[:, 1], epos)
+
+
+def test_inlj_pairs_host_buffers_large(orc, gj, cuda):
+    # 2^24 + 54321 probes from host buffers: every pair in probe order, the
+    # status reads clean
+    import torch
+
+    rng = np.random.default_rng(3)
+    col = column(rng, 1 << 16)
+    m = (1 << 24) + 54321
+    pr = col[rng.integers(0, len(col), m)]
+    pr[::7] = pr[::7] + np.uint64(1)  # some absent keys
+    ix = gj.btree_index().construct(None, to_dev(torch, col))
+    h_pr = torch.from_numpy(pr.view(np.int64).copy()).pin_memory()
+    h_pairs = torch.full((2 * m,), -1, dtype=torch.int32).pin_memory()
+    h_cnt = torch.full((1,), -1, dtype=torch.int64).pin_memory()
+    need = ctypes.c_size_t(0)
+    gj.lib().gj_inlj_pairs_host_workspace_size(m, ctypes.byref(need))
+    ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt, ws)
+    torch.cuda.synchronize()
+    ix.inlj_pairs_status(ws, m)
+    c = int(h_cnt[0])
+    got = h_pairs[: 2 * c].numpy().view(np.uint32).reshape(-1, 2)
+    erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
     np.testing.assert_array_equal(got[:, 0], erows)
     np.testing.assert_array_equal(got[:, 1], epos)
