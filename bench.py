@@ -338,6 +338,14 @@ def inlj_workload(args, world, rank, device, stream):
                 "bytes_per_probe": lookup_bytes_per_probe,
                 "step_bytes_per_probe": bytes_per_probe,
                 "step_achieved": round(bytes_per_probe * m / (step_ms / 1e3) / 1e9, 1)}
+    # index path: the L2 sectors the search pass reads per probe (ncu,
+    # lts__t_sectors_srcunit_tex_op_read at 2^24 probes of the same index),
+    # times 32 B, over the live kernel time
+    l2_sectors = profile_traffic(f"l2_read_sectors_per_probe_k_lookup_{headline_index}_n{args.n_log2}")
+    if l2_sectors:
+        path_gbs = l2_sectors * 32 * m / (lookup_ms / 1e3) / 1e9
+        roofline["index_path"] = {"l2_sectors_per_probe": l2_sectors, "bytes_per_probe": round(l2_sectors * 32, 1),
+                                  "achieved_gbs": round(path_gbs, 1), "frac_of_hbm_peak": round(path_gbs / peak, 4)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
