@@ -41,3 +41,11 @@ def test_load_q14_errors(gj, tmp_path):
     unsorted.write_text("".join(plines))
     with pytest.raises(gj.GJError):
         gj.tpch_load_q14(li, str(unsorted))
+
+
+def test_load_q14_empty_files(gj, tmp_path):
+    li, pa = tmp_path / "lineitem.tbl", tmp_path / "part.tbl"
+    li.write_text("")
+    pa.write_text("")
+    got = gj.tpch_load_q14(str(li), str(pa))
+    assert all(len(v) == 0 for v in got.values())
