@@ -243,3 +243,30 @@ def test_inlj_pairs_host_buffers_large(orc, gj, cuda):
     erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
     np.testing.assert_array_equal(got[:, 0], erows)
     np.testing.assert_array_equal(got[:, 1], epos)
+
+
+@pytest.mark.parametrize("m", [(1 << 22) + 12345, 3 * (1 << 22) + 7])
+def test_inlj_pairs_large(orc, gj, cuda, m):
+    # millions of probes through the two-pass pairs and the allocation-free
+    # entry point: pairs in probe order, clean status
+    import torch
+
+    rng = np.random.default_rng(m % 1000)
+    col = column(rng, 1 << 16)
+    pr = col[rng.integers(0, len(col), m)]
+    pr[::5] = pr[::5] + np.uint64(1)  # absent keys
+    ix = gj.btree_index().construct(None, to_dev(torch, col))
+    d_pr = to_dev(torch, pr)
+    need = ctypes.c_size_t(0)
+    gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(need))
+    ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+    out, cnt = ix.inlj_pairs(d_pr, workspace=ws)
+    ix.inlj_pairs_status(ws, m)
+    rows, pos = pairs_of(out, cnt)
+    erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
+    np.testing.assert_array_equal(rows, erows)
+    np.testing.assert_array_equal(pos, epos)
+    out2, cnt2 = ix.inlj_pairs_noalloc(d_pr, torch.empty_like(out), torch.zeros_like(cnt))
+    rows2, pos2 = pairs_of(out2, cnt2)
+    np.testing.assert_array_equal(rows2, erows)
+    np.testing.assert_array_equal(pos2, epos)
