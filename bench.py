@@ -697,8 +697,9 @@ def learned_workload(args, world, rank, device, stream):
         row = {}
         bs = gj.binary_search_index().construct(None, keys)
         bs.lookup(probes, ref)
-        for kind, kw in (("binary_search", {}), ("radix_spline", {}), ("learned_mlp", {"learned_root": 1}),
-                         ("learned_linear", {"learned_root": 0})):
+        leaves = {"learned_leaves": args.learned_leaves} if args.learned_leaves else {}
+        for kind, kw in (("binary_search", {}), ("radix_spline", {}), ("learned_mlp", {"learned_root": 1, **leaves}),
+                         ("learned_linear", {"learned_root": 0, **leaves})):
             t0 = time.perf_counter()
             ix = gj.make_index(kind.split("_")[0] if kind.startswith("learned") else kind, **kw).construct(None, keys)
             torch.cuda.synchronize()
@@ -883,6 +884,7 @@ def parse_args(argv=None):
                     help="probes per step of --impl reference (all host threads)")
     ap.add_argument("--btree-node-keys", type=int, default=0, help="B+tree inner node width (0 = library default)")
     ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
+    ap.add_argument("--learned-leaves", type=int, default=0, help="learned: leaf models (0 = library default)")
     ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")
     ap.add_argument("--window", type=int, default=0, help="partitioned: window size in probes (0 = autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -525,7 +525,7 @@ void gj_index_params_default(gj_index_params* p) {
     p->rs_max_error = 32;
     p->bs_cache_keys = 4096;
     p->smem_cache_bytes = 16384;
-    p->learned_leaves = 65536;
+    p->learned_leaves = 0;  // about 128 keys per leaf, 2^10 .. 2^20
     p->learned_root = GJ_LEARNED_ROOT_MLP;
     p->learned_hidden = 32;
     p->learned_steps = 600;

@@ -369,8 +369,14 @@ int mlp_grad(const float* d_params, uint32_t H, const float* d_x, const float* d
 int build_learned(gj_index* idx, cudaStream_t s) {
     const gj_index_params& p = idx->params;
     const uint64_t n = idx->n;
-    const uint32_t L = p.learned_leaves;
-    if (L == 0 || L > (1u << 24)) {
+    // leaves: as given, or (0) about 128 keys per leaf -- a power of two in
+    // [2^10, 2^20]; the leaf array (32 B a leaf) stays at most 32 MB
+    uint32_t L = p.learned_leaves;
+    if (L == 0) {
+        L = 1u << 10;
+        while (L < (1u << 20) && (uint64_t)L * 2 * 128 <= n) L <<= 1;
+    }
+    if (L > (1u << 24)) {
         set_error("learned index: leaves must be in [1, 2^24]");
         return GJ_ERR_INVALID_ARGUMENT;
     }

@@ -83,7 +83,8 @@ typedef struct gj_index_params {
     uint32_t rs_max_error;      /* RadixSpline spline error (default 32) */
     uint32_t bs_cache_keys;     /* binary search: sampled keys staged in shared memory (default 4096, 0 = off) */
     uint32_t smem_cache_bytes;  /* B+tree / Harmonia: upper levels staged in shared memory (default 16384) */
-    uint32_t learned_leaves;    /* learned index: linear leaf models (default 65536) */
+    uint32_t learned_leaves;    /* learned index: linear leaf models (default 0: about 128 keys per leaf, a
+                                   power of two in [2^10, 2^20]) */
     uint32_t learned_root;      /* GJ_LEARNED_ROOT_LINEAR or GJ_LEARNED_ROOT_MLP (default MLP) */
     uint32_t learned_hidden;    /* MLP hidden width (default 32, max 32) */
     uint32_t learned_steps;     /* root training steps (default 600) */

@@ -54,7 +54,7 @@ def test_params_defaults(gj):
     assert p.struct_size == ctypes.sizeof(gj.gj_index_params)
     assert p.btree_node_keys == 15 and p.btree_leaf_keys == 4
     assert p.rs_radix_bits == 18 and p.rs_max_error == 32
-    assert p.learned_leaves == 65536 and p.learned_hidden == 32
+    assert p.learned_leaves == 0 and p.learned_hidden == 32
 
 
 def test_argument_errors_without_device(gj):
