@@ -42,6 +42,7 @@ DIST_CLUSTERS = 2
 
 LEARNED_ROOT_LINEAR = 0
 LEARNED_ROOT_MLP = 1
+LEARNED_ROOT_AUTO = 2  # both built, the cheaper linear root kept unless its windows are much wider
 
 
 class GJError(RuntimeError):
@@ -127,6 +128,7 @@ _SIGNATURES = {
     "gj_index_get_type": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "gj_index_size": (_u64, [_vp]),
     "gj_index_learned_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)]),
+    "gj_index_learned_root": (_i32, [_vp, ctypes.POINTER(_u32)]),
     "gj_index_device_view": (_i32, [_vp, _vp, _sz]),
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
@@ -480,6 +482,12 @@ class learned_index(abstract_index):
     """Trained position model (root + linear leaves) with an exact bounded search."""
 
     index_type = index_type_enum.learned
+
+    def root_kind(self) -> int:
+        """LEARNED_ROOT_LINEAR or LEARNED_ROOT_MLP: the root the build kept."""
+        r = _u32(0)
+        _check(lib().gj_index_learned_root(self.handle, ctypes.byref(r)))
+        return r.value
 
     def stats(self) -> Tuple[int, float]:
         me = _u64(0)

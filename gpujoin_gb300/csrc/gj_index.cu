@@ -526,7 +526,7 @@ void gj_index_params_default(gj_index_params* p) {
     p->bs_cache_keys = 4096;
     p->smem_cache_bytes = 16384;
     p->learned_leaves = 0;  // about 128 keys per leaf, 2^10 .. 2^20
-    p->learned_root = GJ_LEARNED_ROOT_MLP;
+    p->learned_root = GJ_LEARNED_ROOT_AUTO;
     p->learned_hidden = 32;
     p->learned_steps = 600;
     p->learned_batch = 8192;
@@ -592,6 +592,25 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
     GJ_CHECK_ARG(p.index_memory == GJ_INDEX_MEMORY_DEVICE || p.index_memory == GJ_INDEX_MEMORY_HOST,
                  "gj_index_build: index_memory must be GJ_INDEX_MEMORY_DEVICE or GJ_INDEX_MEMORY_HOST");
     cudaStream_t s = as_stream(stream);
+    if (type == GJ_INDEX_LEARNED && p.learned_root == GJ_LEARNED_ROOT_AUTO) {
+        // both roots on the same column; the linear one unless its search
+        // windows are much wider (a window of w keys costs about log2(w / 4)
+        // sector loads, the MLP root about a thousand instructions)
+        gj_index_params pl = p, pm = p;
+        pl.learned_root = GJ_LEARNED_ROOT_LINEAR;
+        pm.learned_root = GJ_LEARNED_ROOT_MLP;
+        gj_index *lin = nullptr, *mlp = nullptr;
+        GJ_TRY(gj_index_build(type, d_keys, h_keys, n, &pl, stream, &lin));
+        const int rc = gj_index_build(type, d_keys, h_keys, n, &pm, stream, &mlp);
+        if (rc != GJ_OK) {
+            gj_index_free(lin);
+            return rc;
+        }
+        const bool keep_linear = lin->learned_mean_window <= 2.0 * mlp->learned_mean_window + 16.0;
+        gj_index_free(keep_linear ? mlp : lin);
+        *out_index = keep_linear ? lin : mlp;
+        return GJ_OK;
+    }
     std::unique_ptr<gj_index> idx(new gj_index());
     idx->type = type;
     idx->n = n;
@@ -692,6 +711,16 @@ int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* m
     }
     if (max_error) *max_error = index->learned_max_error;
     if (mean_window) *mean_window = index->learned_mean_window;
+    return GJ_OK;
+}
+
+int gj_index_learned_root(const gj_index* index, uint32_t* root) {
+    GJ_CHECK_ARG(index && root, "gj_index_learned_root: null argument");
+    if (index->type != GJ_INDEX_LEARNED) {
+        set_error("gj_index_learned_root: not a learned index");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    *root = index->params.learned_root;
     return GJ_OK;
 }
 

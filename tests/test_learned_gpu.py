@@ -93,3 +93,23 @@ def test_learned_in_pairs_and_partitioned(orc, gj, cuda):
     erows, epos = orc.pairs_from_positions(exp)
     np.testing.assert_array_equal(got[:, 0], erows)
     np.testing.assert_array_equal(got[:, 1], epos)
+
+
+def test_learned_auto_root(orc, gj, cuda):
+    # the default root is chosen per column: linear on uniform keys (windows
+    # as narrow as the MLP's), the MLP on lognormal keys; lookups stay exact
+    import torch
+
+    from test_lookup_gpu import from_dev_u32
+
+    picks = {}
+    for name, dist in (("uniform", gj.DIST_UNIFORM), ("lognormal", gj.DIST_LOGNORMAL)):
+        keys = gj.generate_sorted_keys(1 << 20, dist, 1 << 63, seed=17)
+        probes = gj.generate_probes(keys, 1 << 18, theta=0.0, absent_fraction=0.05, seed=18)
+        ix = gj.learned_index().construct(None, keys)
+        assert ix.params.learned_root == gj.LEARNED_ROOT_AUTO
+        picks[name] = {gj.LEARNED_ROOT_LINEAR: "linear", gj.LEARNED_ROOT_MLP: "mlp"}[ix.root_kind()]
+        h_keys = keys.cpu().numpy().view(np.uint64)
+        got = from_dev_u32(ix.lookup(probes))
+        np.testing.assert_array_equal(got, orc.bs_lookup(h_keys, probes.cpu().numpy().view(np.uint64)))
+    assert picks == {"uniform": "linear", "lognormal": "mlp"}, picks
