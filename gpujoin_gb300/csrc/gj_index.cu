@@ -421,25 +421,30 @@ int build_radix_spline_index(gj_index* idx, const uint64_t* h_keys, cudaStream_t
     GJ_TRY(host_copy_of_column(idx->d_col, h_keys, idx->n, &store, &col));
     radix_spline_arrays rs;
     GJ_TRY(build_radix_spline(col, idx->n, idx->params.rs_radix_bits, idx->params.rs_max_error, &rs));
-    void *pt = nullptr, *px = nullptr, *py = nullptr;
+    // points with the slope of their segment (the estimate's division, done once)
+    std::vector<rs_point> pts(rs.sx.size());
+    for (size_t i = 0; i < pts.size(); ++i) {
+        pts[i].x = rs.sx[i];
+        pts[i].y = rs.sy[i];
+        pts[i].slope = i + 1 < pts.size() ? (rs.sy[i + 1] - rs.sy[i]) / (double)(rs.sx[i + 1] - rs.sx[i]) : 0.0;
+        pts[i].pad = 0;
+    }
+    void *pt = nullptr, *pp = nullptr;
     GJ_TRY(device_alloc(idx, rs.table.size() * sizeof(uint32_t), &pt));
-    GJ_TRY(device_alloc(idx, rs.sx.size() * sizeof(uint64_t), &px));
-    GJ_TRY(device_alloc(idx, rs.sy.size() * sizeof(double), &py));
+    GJ_TRY(device_alloc(idx, pts.size() * sizeof(rs_point), &pp));
     GJ_CUDA_TRY(cudaMemcpyAsync(pt, rs.table.data(), rs.table.size() * sizeof(uint32_t), cudaMemcpyDefault, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(px, rs.sx.data(), rs.sx.size() * sizeof(uint64_t), cudaMemcpyDefault, s));
-    GJ_CUDA_TRY(cudaMemcpyAsync(py, rs.sy.data(), rs.sy.size() * sizeof(double), cudaMemcpyDefault, s));
+    GJ_CUDA_TRY(cudaMemcpyAsync(pp, pts.data(), pts.size() * sizeof(rs_point), cudaMemcpyDefault, s));
     GJ_CUDA_TRY(cudaStreamSynchronize(s));
     idx->rs.col = idx->d_col;
     idx->rs.n = idx->n;
     idx->rs.table = static_cast<uint32_t*>(pt);
-    idx->rs.sx = static_cast<uint64_t*>(px);
-    idx->rs.sy = static_cast<double*>(py);
+    idx->rs.pts = static_cast<const rs_point*>(pp);
     idx->rs.min_key = rs.min_key;
     idx->rs.max_key = rs.max_key;
     idx->rs.shift = rs.shift;
     idx->rs.max_error = idx->params.rs_max_error;
     idx->rs.col_aligned = aligned32(idx->d_col);
-    idx->bytes = rs.table.size() * sizeof(uint32_t) + rs.sx.size() * (sizeof(uint64_t) + sizeof(double));
+    idx->bytes = rs.table.size() * sizeof(uint32_t) + pts.size() * sizeof(rs_point);
     return GJ_OK;
 }
 

@@ -649,12 +649,22 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
 // ---------------------------------------------------------------------------
 // RadixSpline (src/rs.cuh:118-154, window src/indexes.cuh:205-215)
 // ---------------------------------------------------------------------------
+// A spline point (src/rs.cuh:22-52: Coord{x, y}) with the slope of the
+// segment to the next point, computed at build with the same double
+// division the estimate would make: one 32-byte sector, one load per segment.
+struct rs_point {
+    uint64_t x;
+    double y;
+    double slope;  // (y[i+1] - y[i]) / (x[i+1] - x[i]); 0 for the last point
+    uint64_t pad;
+};
+static_assert(sizeof(rs_point) == 32, "a spline point is one sector");
+
 struct rs_view {
     const uint64_t* col;
     uint64_t n;
     const uint32_t* table;   // (1 << radix_bits) + 2 entries
-    const uint64_t* sx;      // spline point keys
-    const double* sy;        // spline point positions
+    const rs_point* pts;     // spline points, 32-byte aligned
     uint64_t min_key, max_key;
     uint32_t shift;
     uint32_t max_error;
@@ -672,17 +682,18 @@ GJ_DEVICE_INLINE double rs_estimate(const rs_view& v, uint64_t key) {
     uint32_t lo = b, cnt = e - b;
     while (cnt > 0) {
         const uint32_t step = cnt >> 1, mid = lo + step;
-        if (ld_ro(v.sx + mid) < key) {
+        if (ld_ro(&v.pts[mid].x) < key) {
             lo = mid + 1;
             cnt -= step + 1;
         } else {
             cnt = step;
         }
     }
-    const uint64_t dx0 = ld_ro(v.sx + lo - 1), ux = ld_ro(v.sx + lo);
-    const double dy0 = ld_ro(v.sy + lo - 1), uy = ld_ro(v.sy + lo);
-    const double slope = (uy - dy0) / (double)(ux - dx0);
-    return __dadd_rn(__dmul_rn((double)(key - dx0), slope), dy0);
+    // segment [lo - 1, lo]: its left point and precomputed slope
+    uint64_t w[4];
+    ld_sector(reinterpret_cast<const uint64_t*>(v.pts + lo - 1), w);
+    return __dadd_rn(__dmul_rn((double)(key - w[0]), __longlong_as_double((long long)w[2])),
+                     __longlong_as_double((long long)w[1]));
 }
 
 // lower bound inside [b, e), widened to the whole column when the window
