@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 L2_BYTES = 126 * 1024 * 1024
 FALLBACK_HBM_GBS = 6800.0
+ROOT_NAMES = {0: "linear", 1: "mlp", 3: "segments"}  # learned-index root kinds
 
 
 # ---------------------------------------------------------------------------
@@ -699,8 +700,9 @@ def learned_workload(args, world, rank, device, stream):
         bs.lookup(probes, ref)
         leaves = {"learned_leaves": args.learned_leaves} if args.learned_leaves else {}
         for kind, kw in (("binary_search", {}), ("radix_spline", {}), ("learned", dict(leaves)),
-                         ("learned_mlp", {"learned_root": 1, **leaves}),
-                         ("learned_linear", {"learned_root": 0, **leaves})):
+                         ("learned_mlp", {"learned_root": gj.LEARNED_ROOT_MLP, **leaves}),
+                         ("learned_segments", {"learned_root": gj.LEARNED_ROOT_SEGMENTS, **leaves}),
+                         ("learned_linear", {"learned_root": gj.LEARNED_ROOT_LINEAR, **leaves})):
             t0 = time.perf_counter()
             ix = gj.make_index(kind.split("_")[0] if kind.startswith("learned") else kind, **kw).construct(None, keys)
             torch.cuda.synchronize()
@@ -712,7 +714,7 @@ def learned_workload(args, world, rank, device, stream):
             if kind.startswith("learned"):
                 me, mw = ix.stats()
                 entry.update({"max_error": me, "mean_window": round(mw, 2),
-                              "root": "mlp" if ix.root_kind() == gj.LEARNED_ROOT_MLP else "linear"})
+                              "root": ROOT_NAMES[ix.root_kind()]})
             row[kind] = entry
             ix.free()
         # RadixSpline at the learned model's recorded error bound (equal epsilon)

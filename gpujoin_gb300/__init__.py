@@ -42,7 +42,8 @@ DIST_CLUSTERS = 2
 
 LEARNED_ROOT_LINEAR = 0
 LEARNED_ROOT_MLP = 1
-LEARNED_ROOT_AUTO = 2  # both built, the cheaper linear root kept unless its windows are much wider
+LEARNED_ROOT_AUTO = 2  # all roots built, the cheapest kept unless its windows are much wider
+LEARNED_ROOT_SEGMENTS = 3  # piecewise-linear CDF over 4096 equal-width key segments
 
 
 class GJError(RuntimeError):
@@ -484,7 +485,8 @@ class learned_index(abstract_index):
     index_type = index_type_enum.learned
 
     def root_kind(self) -> int:
-        """LEARNED_ROOT_LINEAR or LEARNED_ROOT_MLP: the root the build kept."""
+        """LEARNED_ROOT_LINEAR, LEARNED_ROOT_MLP or LEARNED_ROOT_SEGMENTS: the
+        root the build kept."""
         r = _u32(0)
         _check(lib().gj_index_learned_root(self.handle, ctypes.byref(r)))
         return r.value

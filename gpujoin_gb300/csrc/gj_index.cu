@@ -598,22 +598,39 @@ int gj_index_build(int type, const uint64_t* d_keys, const uint64_t* h_keys, uin
                  "gj_index_build: index_memory must be GJ_INDEX_MEMORY_DEVICE or GJ_INDEX_MEMORY_HOST");
     cudaStream_t s = as_stream(stream);
     if (type == GJ_INDEX_LEARNED && p.learned_root == GJ_LEARNED_ROOT_AUTO) {
-        // both roots on the same column; the linear one unless its search
-        // windows are much wider (a window of w keys costs about log2(w / 4)
-        // sector loads, the MLP root about a thousand instructions)
-        gj_index_params pl = p, pm = p;
-        pl.learned_root = GJ_LEARNED_ROOT_LINEAR;
-        pm.learned_root = GJ_LEARNED_ROOT_MLP;
-        gj_index *lin = nullptr, *mlp = nullptr;
-        GJ_TRY(gj_index_build(type, d_keys, h_keys, n, &pl, stream, &lin));
-        const int rc = gj_index_build(type, d_keys, h_keys, n, &pm, stream, &mlp);
-        if (rc != GJ_OK) {
-            gj_index_free(lin);
-            return rc;
+        // the roots in order of lookup cost -- linear, the segment table (one
+        // L1 load more), a 16-wide MLP, a 32-wide MLP -- on the same column;
+        // the cheapest whose mean search window is at most twice the
+        // narrowest + 16 keys is kept (a window of w keys costs about
+        // log2(w / 4) sector loads, a 32-wide root about a thousand
+        // instructions, a 16-wide one a quarter of that)
+        constexpr int kCand = 4;
+        const uint32_t roots[kCand] = {GJ_LEARNED_ROOT_LINEAR, GJ_LEARNED_ROOT_SEGMENTS, GJ_LEARNED_ROOT_MLP,
+                                       GJ_LEARNED_ROOT_MLP};
+        const uint32_t widths[kCand] = {0, 0, 16, 32};
+        gj_index* cand[kCand] = {nullptr, nullptr, nullptr, nullptr};
+        for (int i = 0; i < kCand; ++i) {
+            gj_index_params pc = p;
+            pc.learned_root = roots[i];
+            if (widths[i]) pc.learned_hidden = widths[i];
+            const int rc = gj_index_build(type, d_keys, h_keys, n, &pc, stream, &cand[i]);
+            if (rc != GJ_OK) {
+                for (gj_index* c : cand) gj_index_free(c);
+                return rc;
+            }
         }
-        const bool keep_linear = lin->learned_mean_window <= 2.0 * mlp->learned_mean_window + 16.0;
-        gj_index_free(keep_linear ? mlp : lin);
-        *out_index = keep_linear ? lin : mlp;
+        double best = cand[0]->learned_mean_window;
+        for (gj_index* c : cand) best = c->learned_mean_window < best ? c->learned_mean_window : best;
+        int keep = kCand - 1;
+        for (int i = 0; i < kCand; ++i) {
+            if (cand[i]->learned_mean_window <= 2.0 * best + 16.0) {
+                keep = i;
+                break;
+            }
+        }
+        for (int i = 0; i < kCand; ++i)
+            if (i != keep) gj_index_free(cand[i]);
+        *out_index = cand[keep];
         return GJ_OK;
     }
     std::unique_ptr<gj_index> idx(new gj_index());

@@ -1,5 +1,6 @@
 // gj_learned.cu -- learned position model: a root model (1 -> H -> H -> 1 ReLU
-// MLP, or a linear model) routes a key to one of L linear leaf models; the
+// MLP, a linear model, or a table of equal-width key segments with the CDF at
+// their ends) routes a key to one of L linear leaf models; the
 // leaf predicts the position and a recorded error window bounds an exact
 // search (device side in gpujoin/device.cuh: learned_lookup).
 //
@@ -10,6 +11,7 @@
 //   k_reduce_partials   sum of the block partials -> gradient
 //   k_adam              Adam step
 //   k_linear_sums       least-squares sums for the linear root
+//   k_segment_ends      positions of the segment ends of the segment-table root
 //   k_route             leaf of every build key (the lookup's own arithmetic)
 //   k_leaf_params       leaf anchors (first key, position) and slopes
 //   k_leaf_error        largest under/over-prediction per leaf
@@ -289,6 +291,31 @@ __global__ void k_leaf_error(learned_view v, const uint32_t* __restrict__ leaf_o
     }
 }
 
+// position of the first key >= the start of segment k (k in [0, S]) of the
+// key range [min_key, max_key] cut into S equal-width segments; S itself ends
+// at n
+__global__ void k_segment_ends(const uint64_t* __restrict__ col, uint64_t n, uint64_t min_key, uint64_t max_key,
+                               uint32_t S, uint64_t* __restrict__ pos) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > S) return;
+    if (k == S) {
+        pos[k] = n;
+        return;
+    }
+    // min_key + floor(k * range / S) without overflow: S is a power of two
+    const uint64_t range = max_key - min_key;
+    const uint64_t key = min_key + (range / S) * k + ((range % S) * k) / S;
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        if (col[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    pos[k] = lo;
+}
+
 int grid_for_n(uint64_t n) {
     uint64_t g = (n + 255) / 256;
     return (int)std::min<uint64_t>(g ? g : 1, 4096);
@@ -380,7 +407,8 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         set_error("learned index: leaves must be in [1, 2^24]");
         return GJ_ERR_INVALID_ARGUMENT;
     }
-    if (p.learned_root != GJ_LEARNED_ROOT_LINEAR && p.learned_root != GJ_LEARNED_ROOT_MLP) {
+    if (p.learned_root != GJ_LEARNED_ROOT_LINEAR && p.learned_root != GJ_LEARNED_ROOT_MLP &&
+        p.learned_root != GJ_LEARNED_ROOT_SEGMENTS) {
         set_error("learned index: unknown root model");
         return GJ_ERR_INVALID_ARGUMENT;
     }
@@ -403,9 +431,13 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     v.root_kind = p.learned_root;
     v.hidden = H;
     v.col_aligned = column_aligned32(idx->d_col);
+    const bool segments = p.learned_root == GJ_LEARNED_ROOT_SEGMENTS;
+    v.segments = segments ? kLearnedSegments : 0;
 
     const uint32_t np = p.learned_root == GJ_LEARNED_ROOT_MLP ? mlp_param_count(H) : 2;  // trained parameters
-    const uint32_t nstored = p.learned_root == GJ_LEARNED_ROOT_MLP ? (uint32_t)kMlpParams : 2u;
+    const uint32_t nstored = p.learned_root == GJ_LEARNED_ROOT_MLP ? (uint32_t)kMlpParams
+                             : segments                           ? 2 * kLearnedSegments
+                                                                  : 2u;
     void* root_mem = nullptr;
     void* leaf_mem = nullptr;
     GJ_TRY(device_alloc_for(idx, nstored * sizeof(float), &root_mem));
@@ -418,6 +450,26 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     std::memset(&idx->ln_root, 0, sizeof(idx->ln_root));
 
     scratch sc;
+    if (segments) {
+        // y = position / n at every segment end; a segment holds {y, dy}
+        const uint32_t S = kLearnedSegments;
+        uint64_t* d_pos = nullptr;
+        GJ_TRY(sc.alloc(S + 1, &d_pos));
+        k_segment_ends<<<(S + 1 + 255) / 256, 256, 0, s>>>(idx->d_col, n, v.min_key, v.max_key, S, d_pos);
+        GJ_CUDA_TRY(cudaGetLastError());
+        std::vector<uint64_t> pos(S + 1);
+        GJ_CUDA_TRY(cudaMemcpyAsync(pos.data(), d_pos, pos.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+        std::vector<float> table(2 * S);
+        for (uint32_t i = 0; i < S; ++i) {
+            const double y0 = (double)pos[i] / (double)n, y1 = (double)pos[i + 1] / (double)n;
+            table[2 * i] = (float)y0;
+            table[2 * i + 1] = (float)(y1 - y0);
+        }
+        GJ_CUDA_TRY(cudaMemcpyAsync(d_root, table.data(), table.size() * sizeof(float), cudaMemcpyDefault, s));
+        // the table's copy must land before `table` goes out of scope
+        GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    }
     // training samples
     const uint64_t S = std::min<uint64_t>(n, 1u << 20);
     float *xs = nullptr, *ys = nullptr;
@@ -447,7 +499,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         const double b = (sy - a * sx) / N;
         idx->ln_root.w[0] = (float)a;
         idx->ln_root.w[1] = (float)b;
-    } else {
+    } else if (!segments) {
         // start from the piecewise-linear CDF through H + 1 sample quantiles
         std::vector<float> hx(S), hy(S);
         GJ_CUDA_TRY(cudaMemcpyAsync(hx.data(), xs, S * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -521,7 +573,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         }
         out[4 * W + W * W] = best[4 * H + H * H];  // b3
     }
-    GJ_CUDA_TRY(cudaMemcpyAsync(d_root, idx->ln_root.w, nstored * sizeof(float), cudaMemcpyDefault, s));
+    if (!segments) GJ_CUDA_TRY(cudaMemcpyAsync(d_root, idx->ln_root.w, nstored * sizeof(float), cudaMemcpyDefault, s));
 
     // route every key, fit the leaves, measure their error windows
     uint32_t* leaf_of = nullptr;
@@ -533,7 +585,9 @@ int build_learned(gj_index* idx, cudaStream_t s) {
     GJ_CUDA_TRY(cudaMemsetAsync(first, 0xFF, L * sizeof(unsigned int), s));
     GJ_CUDA_TRY(cudaMemsetAsync(last, 0, L * sizeof(unsigned int), s));
     GJ_CUDA_TRY(cudaMemsetAsync(count, 0, L * sizeof(unsigned int), s));
-    k_route<<<grid_for_n(n), 256, nstored * sizeof(float), s>>>(v, v.root, leaf_of, first, last, count);
+    // k_route stages the by-value parameters (none for the segment table)
+    const size_t route_smem = (p.learned_root == GJ_LEARNED_ROOT_MLP ? kMlpParams : 2) * sizeof(float);
+    k_route<<<grid_for_n(n), 256, route_smem, s>>>(v, v.root, leaf_of, first, last, count);
     k_leaf_params<<<(L + 255) / 256, 256, 0, s>>>(idx->d_col, L, first, last, count,
                                                  const_cast<learned_leaf*>(v.leaves));
     k_leaf_error<<<grid_for_n(n), 256, 0, s>>>(v, leaf_of, const_cast<learned_leaf*>(v.leaves));

@@ -67,8 +67,11 @@ typedef enum gj_index_type {
 
 #define GJ_LEARNED_ROOT_LINEAR 0u
 #define GJ_LEARNED_ROOT_MLP 1u
-#define GJ_LEARNED_ROOT_AUTO 2u /* both are built; the linear root is kept unless its mean search window
-                                   is over twice the MLP's (+16 keys): it costs far fewer instructions */
+#define GJ_LEARNED_ROOT_AUTO 2u /* a linear root, a segment table, a 16-wide and a 32-wide MLP are built, in
+                                   that order of lookup cost; the cheapest whose mean search window is at
+                                   most twice the narrowest (+16 keys) is kept */
+#define GJ_LEARNED_ROOT_SEGMENTS 3u /* piecewise-linear CDF over 4096 equal-width key segments, exact at the
+                                       segment ends: one table load and one FMA per lookup */
 
 /* Build parameters.  Call gj_index_params_default() first, then override.
  * Replaces the compile-time IndexConfiguration / constants of the reference
@@ -87,8 +90,7 @@ typedef struct gj_index_params {
     uint32_t smem_cache_bytes;  /* B+tree / Harmonia: upper levels staged in shared memory (default 16384) */
     uint32_t learned_leaves;    /* learned index: linear leaf models (default 0: about 128 keys per leaf, a
                                    power of two in [2^10, 2^20]) */
-    uint32_t learned_root;      /* GJ_LEARNED_ROOT_LINEAR, GJ_LEARNED_ROOT_MLP or GJ_LEARNED_ROOT_AUTO
-                                   (default AUTO) */
+    uint32_t learned_root;      /* GJ_LEARNED_ROOT_LINEAR, _MLP, _SEGMENTS or _AUTO (default AUTO) */
     uint32_t learned_hidden;    /* MLP hidden width (default 32, max 32) */
     uint32_t learned_steps;     /* root training steps (default 600) */
     uint32_t learned_batch;     /* root training batch (default 8192) */
@@ -135,8 +137,8 @@ uint64_t gj_index_size(const gj_index* index);
 /* learned index: recorded maximum prediction error (positions) and mean
  * search-window width over the build keys */
 int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* mean_window);
-/* the root model a learned index was built with (GJ_LEARNED_ROOT_LINEAR or
- * _MLP; the one kept when the build asked for GJ_LEARNED_ROOT_AUTO) */
+/* the root model a learned index was built with (GJ_LEARNED_ROOT_LINEAR,
+ * _MLP or _SEGMENTS; the one kept when the build asked for GJ_LEARNED_ROOT_AUTO) */
 int gj_index_learned_root(const gj_index* index, uint32_t* root);
 
 /* The index's device view -- the struct passed by value to kernels, like

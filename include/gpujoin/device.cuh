@@ -740,10 +740,11 @@ struct learned_leaf {
 };
 static_assert(sizeof(learned_leaf) == 32, "a leaf is one sector");
 
-// The root MLP is always evaluated 32 wide: 1 -> 32 -> 32 -> 1 with ReLU over
+// The root MLP is stored 32 wide: 1 -> 32 -> 32 -> 1 with ReLU over
 // [W1(32) b1(32) W2(32x32, out-major) b2(32) W3(32) b3].  Narrower trained
 // networks are stored zero-padded; the padding adds exact zeros, so the
-// result is the narrower network's.
+// result is the narrower network's, and one of at most 16 units is
+// evaluated over its first 16 lanes only.
 constexpr int kMlpWidth = 32;
 constexpr int kMlpParams = 2 * kMlpWidth + kMlpWidth * kMlpWidth + 2 * kMlpWidth + 1;  // 1153
 
@@ -753,13 +754,17 @@ struct learned_view {
     uint64_t min_key, max_key;
     float inv_range;            // 1 / (max_key - min_key) (0 if the range is empty)
     uint32_t num_leaves;
-    uint32_t root_kind;         // GJ_LEARNED_ROOT_LINEAR or GJ_LEARNED_ROOT_MLP
+    uint32_t root_kind;         // GJ_LEARNED_ROOT_LINEAR, _MLP or _SEGMENTS
     uint32_t hidden;            // trained MLP width H (<= 32), stored padded to 32
-    const float* root;          // [a, b] (linear) or kMlpParams MLP parameters
+    const float* root;          // [a, b] (linear), kMlpParams MLP parameters or
+                                // the segment table ({y, dy} per segment)
     const learned_leaf* leaves; // 32-byte aligned
     uint32_t col_aligned;       // column base is 32-byte aligned
-    uint32_t pad;
+    uint32_t segments;          // segment-table root: number of segments
 };
+
+// segments of the segment-table root (a 32 KB table: it stays in L1)
+constexpr uint32_t kLearnedSegments = 4096;
 
 // root parameters carried by value (a kernel argument): the forward pass then
 // reads its weights as constant-bank operands of its FMAs
@@ -774,25 +779,29 @@ GJ_DEVICE_INLINE float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a
 // of packed FMAs (out = b2 + even + odd), half the instructions of a scalar
 // chain; the build routes keys with this same function, so the recorded
 // error windows hold for it.  P must be 8-byte aligned.
-GJ_DEVICE_INLINE float mlp32_forward(const float* P, float x) {
-    constexpr int H = kMlpWidth;
+template <int H>
+GJ_DEVICE_INLINE float mlp_forward(const float* P, float x) {
+    // H: evaluated width (16 or 32) over the 32-wide stored layout; for a
+    // network of at most 16 units the lanes 16..31 are exact zeros, so both
+    // widths give the same result and the 16-wide one a quarter of layer 2
+    constexpr int W = kMlpWidth;
     const float2* W1 = reinterpret_cast<const float2*>(P);
-    const float2* b1 = reinterpret_cast<const float2*>(P + H);
+    const float2* b1 = reinterpret_cast<const float2*>(P + W);
     float2 h1[H / 2];
 #pragma unroll
     for (int j = 0; j < H / 2; ++j) {
         const float2 a = fma2(W1[j], make_float2(x, x), b1[j]);
         h1[j] = make_float2(a.x > 0.f ? a.x : 0.f, a.y > 0.f ? a.y : 0.f);
     }
-    float out = P[4 * H + H * H];  // b3
+    float out = P[4 * W + W * W];  // b3
 #pragma unroll
     for (int o = 0; o < H; ++o) {
-        const float2* w = reinterpret_cast<const float2*>(P + 2 * H + o * H);
+        const float2* w = reinterpret_cast<const float2*>(P + 2 * W + o * W);
         float2 s = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < H / 2; ++j) s = fma2(w[j], h1[j], s);
-        const float a = P[2 * H + H * H + o] + s.x + s.y;  // b2[o] + even + odd
-        out = fmaf(P[3 * H + H * H + o], a > 0.f ? a : 0.f, out);
+        const float a = P[2 * W + W * W + o] + s.x + s.y;  // b2[o] + even + odd
+        out = fmaf(P[3 * W + W * W + o], a > 0.f ? a : 0.f, out);
     }
     return out;
 }
@@ -803,8 +812,22 @@ GJ_DEVICE_INLINE float learned_norm(const learned_view& v, uint64_t key) {
     return (float)(key - v.min_key) * v.inv_range;
 }
 
+// The segment-table root is r(x) = y[i] + (xS - i) * dy[i] with i = floor(xS)
+// over S equal-width segments of the normalised key, y[i] the fraction of keys
+// below segment i's first key: the key CDF, exact at every segment end and
+// linear in between.  It reads the table from global memory (v.root), not
+// from `root`, which holds the by-value parameters of the other kinds.
 GJ_DEVICE_INLINE uint32_t learned_route(const learned_view& v, const float* root, float x) {
-    const float r = (v.root_kind == GJ_LEARNED_ROOT_MLP) ? mlp32_forward(root, x) : fmaf(root[0], x, root[1]);
+    float r;
+    if (v.root_kind == GJ_LEARNED_ROOT_SEGMENTS) {
+        const float t = x * (float)v.segments;
+        const uint32_t i = min((uint32_t)t, v.segments - 1);
+        const float2 s = __ldg(reinterpret_cast<const float2*>(v.root) + i);
+        r = fmaf(t - (float)i, s.y, s.x);
+    } else if (v.root_kind == GJ_LEARNED_ROOT_MLP)
+        r = v.hidden <= 16 ? mlp_forward<16>(root, x) : mlp_forward<32>(root, x);
+    else
+        r = fmaf(root[0], x, root[1]);
     const float lf = floorf(r * (float)v.num_leaves);
     if (!(lf > 0.f)) return 0;  // also catches NaN
     if (lf >= (float)v.num_leaves) return v.num_leaves - 1;

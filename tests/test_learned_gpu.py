@@ -31,7 +31,7 @@ def test_mlp_gradient_matches_oracle(orc, gj, cuda, H):
 
 
 @pytest.mark.parametrize("dist", [0, 1, 2])
-@pytest.mark.parametrize("root", [0, 1])
+@pytest.mark.parametrize("root", [0, 1, 3])
 def test_learned_lookup_exact(orc, gj, cuda, dist, root):
     import torch
 
@@ -58,7 +58,7 @@ def test_learned_small_and_ragged(orc, gj, cuda):
     for n in (1, 2, 3, 100, 4097):
         col = column(rng, n)
         pr = probes_for(rng, col, 500)
-        for root in (0, 1):
+        for root in (0, 1, 3):
             ix = gj.learned_index(learned_root=root, learned_leaves=64, learned_steps=20).construct(None,
                                                                                                   to_dev(torch, col))
             np.testing.assert_array_equal(from_dev_u32(ix.lookup(to_dev(torch, pr))), orc.bs_lookup(col, pr),
@@ -95,9 +95,40 @@ def test_learned_in_pairs_and_partitioned(orc, gj, cuda):
     np.testing.assert_array_equal(got[:, 1], epos)
 
 
+def test_segment_root_beats_linear_root_on_skewed_keys(orc, gj, cuda):
+    # the segment table follows the key CDF: far narrower windows than the
+    # linear root on lognormal and clustered keys; lookups exact
+    for dist in (1, 2):
+        keys = gj.generate_sorted_keys(1 << 20, dist, 1 << 63, seed=70 + dist)
+        lin = gj.learned_index(learned_root=gj.LEARNED_ROOT_LINEAR, learned_leaves=4096).construct(None, keys)
+        seg = gj.learned_index(learned_root=gj.LEARNED_ROOT_SEGMENTS, learned_leaves=4096).construct(None, keys)
+        assert seg.root_kind() == gj.LEARNED_ROOT_SEGMENTS
+        _, w_lin = lin.stats()
+        _, w_seg = seg.stats()
+        assert w_seg < 0.5 * w_lin, (dist, w_seg, w_lin)
+        probes = gj.generate_probes(keys, 1 << 17, theta=0.0, absent_fraction=0.05, seed=71)
+        np.testing.assert_array_equal(from_dev_u32(seg.lookup(probes)),
+                                      orc.bs_lookup(keys.cpu().numpy().view(np.uint64),
+                                                    probes.cpu().numpy().view(np.uint64)))
+
+
+def test_segment_root_host_memory(orc, gj, cuda):
+    # the segment table read from pinned host memory
+    keys = gj.generate_sorted_keys(1 << 18, 1, 1 << 63, seed=81)
+    probes = gj.generate_probes(keys, 1 << 16, theta=0.0, absent_fraction=0.05, seed=82)
+    h_keys = keys.cpu().pin_memory()
+    ix = gj.learned_index(learned_root=gj.LEARNED_ROOT_SEGMENTS, learned_leaves=2048,
+                          index_memory=gj.INDEX_MEMORY_HOST).construct(None, h_keys)
+    assert ix.host_memory() > 0
+    np.testing.assert_array_equal(from_dev_u32(ix.lookup(probes)),
+                                  orc.bs_lookup(keys.cpu().numpy().view(np.uint64),
+                                                probes.cpu().numpy().view(np.uint64)))
+
+
 def test_learned_auto_root(orc, gj, cuda):
     # the default root is chosen per column: linear on uniform keys (windows
-    # as narrow as the MLP's), the MLP on lognormal keys; lookups stay exact
+    # as narrow as any other root's), a root that follows the CDF (segment
+    # table or MLP) on lognormal keys; lookups stay exact
     import torch
 
     from test_lookup_gpu import from_dev_u32
@@ -108,8 +139,9 @@ def test_learned_auto_root(orc, gj, cuda):
         probes = gj.generate_probes(keys, 1 << 18, theta=0.0, absent_fraction=0.05, seed=18)
         ix = gj.learned_index().construct(None, keys)
         assert ix.params.learned_root == gj.LEARNED_ROOT_AUTO
-        picks[name] = {gj.LEARNED_ROOT_LINEAR: "linear", gj.LEARNED_ROOT_MLP: "mlp"}[ix.root_kind()]
+        picks[name] = {gj.LEARNED_ROOT_LINEAR: "linear", gj.LEARNED_ROOT_MLP: "cdf",
+                       gj.LEARNED_ROOT_SEGMENTS: "cdf"}[ix.root_kind()]
         h_keys = keys.cpu().numpy().view(np.uint64)
         got = from_dev_u32(ix.lookup(probes))
         np.testing.assert_array_equal(got, orc.bs_lookup(h_keys, probes.cpu().numpy().view(np.uint64)))
-    assert picks == {"uniform": "linear", "lognormal": "mlp"}, picks
+    assert picks == {"uniform": "linear", "lognormal": "cdf"}, picks
