@@ -214,6 +214,8 @@ def index_params(args, kind):
             p["btree_node_keys"] = args.btree_node_keys
         if args.btree_leaf_keys:
             p["btree_leaf_keys"] = args.btree_leaf_keys
+        if args.btree_start_bits:
+            p["btree_start_bits"] = args.btree_start_bits
     return p
 
 
@@ -887,6 +889,8 @@ def parse_args(argv=None):
     ap.add_argument("--ref-sample", type=int, default=1 << 25,
                     help="probes per step of --impl reference (all host threads)")
     ap.add_argument("--btree-node-keys", type=int, default=0, help="B+tree inner node width (0 = library default)")
+    ap.add_argument("--btree-start-bits", type=int, default=0,
+                    help="B+tree start table bits (0 = library default)")
     ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
     ap.add_argument("--learned-leaves", type=int, default=0, help="learned: leaf models (0 = library default)")
     ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")

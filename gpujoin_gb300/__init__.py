@@ -82,7 +82,7 @@ class gj_index_params(ctypes.Structure):
         ("learned_batch", ctypes.c_uint32),
         ("learned_lr", ctypes.c_float),
         ("index_memory", ctypes.c_uint32),
-        ("reserved0", ctypes.c_uint32),
+        ("btree_start_bits", ctypes.c_uint32),
         ("seed", ctypes.c_uint64),
     ]
 

@@ -80,6 +80,21 @@ __global__ void k_gather_fence(const uint64_t* __restrict__ col, uint64_t n, uin
     }
 }
 
+// start table of a B+tree: entry b = the deepest node shared by the exact
+// descents of every key of bucket b, [min + b * 2^shift, min + (b + 1) * 2^shift)
+// clamped to max (v reads every level from global memory: no shared cache)
+template <int W>
+__global__ void k_btree_start(btree_view v, uint64_t entries, uint64_t* __restrict__ out) {
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < entries;
+         b += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = v.min_key + (b << v.start_shift);
+        const uint64_t hi = b + 1 == entries ? v.max_key : lo + ((1ull << v.start_shift) - 1);
+        const btree_cursor c = btree_common_node<W, false>(v, nullptr, lo, hi);
+        out[2 * b] = c.base;
+        out[2 * b + 1] = (uint64_t)c.node | ((uint64_t)(uint32_t)c.level << 32);
+    }
+}
+
 // B+tree level l, W separators per node, fanout F = W + 1: slot k = (node j,
 // separator c) is the max key of child j*F + c one level down, which covers
 // the column range [child * span, (child + 1) * span); UINT64_MAX past the end
@@ -372,6 +387,46 @@ int build_btree(gj_index* idx, cudaStream_t s) {
     idx->bt.max_key = maxk;
     idx->bt.min_key = min_key;
     idx->bytes = total * sizeof(uint64_t);
+
+    // start table: by default about one bucket per 64 keys (2^1 .. 2^20
+    // buckets, at most 16 MB), so that most buckets lie inside one node two
+    // levels above the leaves; finer tables (measured at 2^21 - 2^23 buckets
+    // for 2^26 keys) fall out of L2 and make every start a DRAM access
+    uint32_t R = idx->params.btree_start_bits;
+    if (R > 24) {
+        set_error("btree: start table bits must be at most 24");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (R == 0) {
+        R = 1;
+        while (R < 20 && (n >> (R + 7)) != 0) ++R;
+    }
+    const uint64_t range = maxk - min_key;
+    const uint32_t used = range ? 64u - (uint32_t)__builtin_clzll(range) : 0u;
+    const uint32_t shift = used > R ? used - R : 0u;
+    const uint64_t entries = (range >> shift) + 1;
+    void* tp = nullptr;
+    GJ_TRY(device_alloc(idx, entries * 16, &tp));
+    btree_view tv = idx->bt;
+    tv.cached_levels = 0;
+    tv.start_shift = shift;
+    const int grid = (int)std::min<uint64_t>((entries + 255) / 256, 4096);
+    uint64_t* table = static_cast<uint64_t*>(tp);
+    switch (W) {
+        case 4: k_btree_start<4><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        case kBtreeCompressed: k_btree_start<kBtreeCompressed><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        case 8: k_btree_start<8><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        case kBtreeCompressed16: k_btree_start<kBtreeCompressed16><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        case 16: k_btree_start<16><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        case 32: k_btree_start<32><<<grid, 256, 0, s>>>(tv, entries, table); break;
+        default: k_btree_start<64><<<grid, 256, 0, s>>>(tv, entries, table); break;
+    }
+    GJ_CUDA_TRY(cudaGetLastError());
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    idx->bt.start = table;
+    idx->bt.start_shift = shift;
+    idx->bt.start_entries = (uint32_t)entries;
+    idx->bytes += entries * 16;
     return GJ_OK;
 }
 

@@ -84,6 +84,18 @@ GJ_DEVICE_INLINE void ld_sector_c(const uint64_t* p, uint64_t (&k)[4]) {
     }
 }
 
+// 16 bytes (p 16-byte aligned) under the L2 class, 64-byte fill on a miss
+template <int kClass>
+GJ_DEVICE_INLINE void ld_pair_c(const uint64_t* p, uint64_t (&k)[2]) {
+    if constexpr (kClass == kL2Default) {
+        asm("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(k[0]), "=l"(k[1]) : "l"(p));
+    } else {
+        asm("ld.global.nc.L2::cache_hint.L2::64B.v2.u64 {%0, %1}, [%2], %3;"
+            : "=l"(k[0]), "=l"(k[1])
+            : "l"(p), "l"(l2_policy<kClass>()));
+    }
+}
+
 template <int kClass>
 GJ_DEVICE_INLINE uint64_t ld_ro_c(const uint64_t* p) {
     if constexpr (kClass == kL2Default) {
@@ -239,6 +251,13 @@ struct btree_view {
     uint32_t node_keys;                     // W (separators per node)
     uint32_t leaf_keys;                     // L
     uint32_t col_aligned;                   // column base is 32-byte aligned
+    // start table: the key range [min_key, max_key] cut into buckets of
+    // 2^start_shift keys; entry b (16 bytes: base, node | level << 32) is the
+    // deepest node every key of bucket b passes, where a lookup starts its
+    // descent (null: from the root)
+    const uint64_t* start;
+    uint32_t start_shift;
+    uint32_t start_entries;
 };
 
 // Compressed nodes (W = 7): a node is one 32-byte sector of 8 uint32 words,
@@ -496,9 +515,15 @@ GJ_DEVICE_INLINE uint32_t btree_lookup_from(const btree_view& v, const uint64_t*
     return eq ? (uint32_t)pos : kInvalid;
 }
 
+// A scattered lookup starts at its key bucket's entry of the start table:
+// one 16-byte load in place of the levels above that node.
 template <int W, bool kScattered = true>
 GJ_DEVICE_INLINE uint32_t btree_lookup(const btree_view& v, const uint64_t* cache, uint64_t key) {
-    return btree_lookup_from<W, kScattered>(v, cache, key, btree_root(v));
+    if (key > v.max_key || key < v.min_key) return kInvalid;
+    if (v.start == nullptr) return btree_lookup_from<W, kScattered>(v, cache, key, btree_root(v));
+    uint64_t e[2];
+    ld_pair_c<kScattered ? kL2Keep : kL2Default>(v.start + 2 * ((key - v.min_key) >> v.start_shift), e);
+    return btree_lookup_from<W, kScattered>(v, cache, key, {e[0], (uint32_t)e[1], (int32_t)(e[1] >> 32)});
 }
 
 // The deepest node on the paths of both lo and hi (lo <= hi): every key in

@@ -128,6 +128,45 @@ def test_btree_compressed_nodes(orc, gj, cuda, node_keys, leaf_keys):
         np.testing.assert_array_equal(got, want, err_msg=f"partitioned {name} W={node_keys} L={leaf_keys}")
 
 
+@pytest.mark.parametrize("node_keys", [4, 7, 15, 64])
+@pytest.mark.parametrize("start_bits", [1, 6, 24])
+def test_btree_start_table(orc, gj, cuda, node_keys, start_bits):
+    # scattered lookups start at their key bucket's deepest shared node: from
+    # two buckets to more buckets than keys, on dense keys, runs with huge
+    # gaps (many empty buckets) and keys next to 2^64 - 1
+    import torch
+
+    rng = np.random.default_rng(node_keys * 31 + start_bits)
+    for name, col in compressed_key_sets(rng).items():
+        col = np.ascontiguousarray(col, dtype=np.uint64)
+        pr = np.concatenate([col, col - np.uint64(1), col + np.uint64(1),
+                             rng.integers(0, 1 << 63, 5000, dtype=np.uint64) * np.uint64(2),
+                             np.array([0, 1, (1 << 64) - 1, (1 << 64) - 2, 1 << 63], dtype=np.uint64)])
+        ix = gj.btree_index(btree_node_keys=node_keys, btree_start_bits=start_bits).construct(None,
+                                                                                            to_dev(torch, col))
+        got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
+        np.testing.assert_array_equal(got, orc.exact_lookup(col, pr),
+                                      err_msg=f"{name} W={node_keys} start bits {start_bits}")
+
+
+def test_btree_start_table_size(gj, cuda):
+    import torch
+
+    # 16 bytes per bucket; buckets of 2^shift keys cover [min, max]
+    col = torch.arange(0, 1 << 16, dtype=torch.int64, device="cuda") * 5
+    key_range = 5 * ((1 << 16) - 1)
+
+    def entries(bits):
+        shift = max(0, key_range.bit_length() - bits)
+        return (key_range >> shift) + 1
+
+    small = gj.btree_index(btree_start_bits=4).construct(None, col).memory_consumption()
+    large = gj.btree_index(btree_start_bits=16).construct(None, col).memory_consumption()
+    assert large - small == (entries(16) - entries(4)) * 16
+    with pytest.raises(gj.GJError):
+        gj.btree_index(btree_start_bits=25).construct(None, col)
+
+
 def test_unaligned_column(orc, gj, cuda):
     # columns that start 8 and 16 bytes into an allocation: 32-byte sector loads must not be used
     import torch
