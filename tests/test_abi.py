@@ -33,6 +33,42 @@ def test_bindings_cover_header(gj):
     assert sorted(gj.exported_symbols()) == declared_functions()
 
 
+_C_TYPES = {"uint8_t": ctypes.c_uint8, "uint32_t": ctypes.c_uint32, "uint64_t": ctypes.c_uint64,
+            "int64_t": ctypes.c_int64, "float": ctypes.c_float}
+
+
+def declared_structs():
+    """{name: [(field, C type, is_pointer)]} of every struct defined in the header."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for name, body in re.findall(r"typedef struct (\w+) \{(.*?)\} \1;", text, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            ctype, names = decl.split(None, 1)
+            for f in names.split(","):
+                f = f.strip()
+                fields.append((f.lstrip("*"), ctype, f.startswith("*") or ctype.endswith("*")))
+        out[name] = fields
+    return out
+
+
+def test_struct_mirrors_match_header(gj):
+    # every struct of the ABI: the ctypes mirror has the header's fields, in
+    # order, with the same types (a renamed or reordered field would pass
+    # wrong values silently)
+    structs = declared_structs()
+    assert set(structs) == {"gj_index_params", "gj_q14_tables"}
+    for name, fields in structs.items():
+        mirror = getattr(gj, name)._fields_
+        assert [f for f, _ in mirror] == [f for f, _, _ in fields], name
+        for (f, ct), (_, c_type, ptr) in zip(mirror, fields):
+            want = _C_TYPES[c_type.rstrip("*")]
+            assert ct == (ctypes.POINTER(want) if ptr else want), (name, f)
+
+
 def test_abi_version_and_names(gj):
     L = gj.lib()
     assert L.gj_abi_version() == 1
@@ -55,6 +91,7 @@ def test_params_defaults(gj):
     assert p.btree_node_keys == 15 and p.btree_leaf_keys == 4
     assert p.rs_radix_bits == 18 and p.rs_max_error == 32
     assert p.learned_leaves == 0 and p.learned_hidden == 32
+    assert p.learned_root == gj.LEARNED_ROOT_AUTO and p.btree_start_bits == 0
 
 
 def test_argument_errors_without_device(gj):
