@@ -206,6 +206,64 @@ def cpu_baseline_btree(h_keys, h_probes, sample: int):
                       f"(oracle B+tree, reference page geometry 247/246), {threads} threads, {dt:.2f} s"}
 
 
+# ---------------------------------------------------------------------------
+# parity against the oracle, outside every timed region
+# ---------------------------------------------------------------------------
+def oracle_positions(h_keys, h_probes):
+    """(lower bound, exact) oracle positions of every probe, all host threads
+    (the oracle's B+tree restatement; equal to its binary search)."""
+    import oracle
+
+    return oracle.fast_positions(h_keys, h_probes, oracle.hardware_threads())
+
+
+def check_pairs(pairs, count, expect, ordered=True):
+    """Compare GPU join pairs with the oracle's positions per probe row
+    (expect: int32 device tensor, -1 = no match).  ordered: pairs in probe
+    order; otherwise as a set (partitioned pairs).  Device-side compare."""
+    import torch
+
+    got = int(count.item())
+    rows = torch.nonzero(expect != -1).squeeze(1)
+    n_exp = rows.numel()
+    if got != n_exp:
+        return {"checked": n_exp, "mismatches": max(abs(got - n_exp), 1), "count": got, "expected_count": n_exp}
+    p = pairs[: 2 * got].view(-1, 2)
+    if ordered:
+        bad = int(((p[:, 0].long() != rows) | (p[:, 1] != expect[rows])).sum())
+    else:
+        by_row = torch.full_like(expect, -1)
+        by_row[p[:, 0].long()] = p[:, 1]
+        bad = int((by_row != expect).sum())
+    return {"checked": got, "mismatches": bad}
+
+
+def check_pairs_sample(pairs, count, m, h_keys, h_probes, sample, seed, semantics="exact"):
+    """Partitioned pairs of m probes against the oracle on a seeded sample of
+    probe rows (plus the pair count): the pairs are gathered by row on the
+    device, the oracle searches the sampled rows on the host."""
+    import numpy as np
+    import torch
+
+    import oracle
+
+    got = int(count.item())
+    p = pairs[: 2 * got].view(-1, 2)
+    by_row = torch.full((m,), -1, dtype=torch.int32, device=pairs.device)
+    by_row[p[:, 0].long()] = p[:, 1]
+    rng = np.random.default_rng(seed)
+    rows = np.unique(rng.integers(0, m, size=sample))
+    lb, ex = oracle.fast_positions(h_keys, h_probes[rows], oracle.hardware_threads())
+    want = (ex if semantics == "exact" else lb).view(np.int32)
+    have = by_row[torch.from_numpy(rows).to(pairs.device)].cpu().numpy()
+    matched_rows = int((by_row != -1).sum())
+    return {"checked": int(len(rows)), "mismatches": int(np.count_nonzero(have != want)), "count": got,
+            "rows_with_a_pair": matched_rows, "sample": f"{len(rows)} seeded probe rows of {m} + the pair count"}
+
+
+EXACT_KINDS = ("btree", "harmonia", "hash")  # position of an equal key, else none
+
+
 def index_params(args, kind):
     """Build parameters given on the command line for an index kind."""
     p = {}
@@ -254,6 +312,19 @@ def inlj_workload(args, world, rank, device, stream):
 
     kinds = [k.strip() for k in args.indexes.split(",") if k.strip()]
     per_index = {}
+    # oracle positions of every probe (host threads, outside the timed
+    # regions), on the device for the comparisons
+    # (rank 0 only: the replicas' inputs are the same)
+    h_keys = keys.cpu().numpy().view(np.uint64)
+    h_probes = probes.cpu().numpy().view(np.uint64)
+    expect, oracle_s = None, 0.0
+    if rank == 0 and not args.no_parity:
+        t_or = time.perf_counter()
+        lb, ex = oracle_positions(h_keys, h_probes)
+        expect = {"lower_bound": torch.from_numpy(lb.view(np.int32)).to(device),
+                  "exact": torch.from_numpy(ex.view(np.int32)).to(device)}
+        del lb, ex
+        oracle_s = time.perf_counter() - t_or
     headline_ms = None
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
@@ -263,9 +334,14 @@ def inlj_workload(args, world, rank, device, stream):
     headline_index = None
     bytes_per_probe = 8 + 8 + (32 if 8 * n > L2_BYTES else 0)
     clocks = None
-    for kind in kinds:
+    for entry in kinds:
+        # "btree_w64": the B+tree with 64-key uint64 inner nodes (the node
+        # width of the INLJ configuration as written)
+        kind, params = entry, index_params(args, entry)
+        if entry == "btree_w64":
+            kind, params = "btree", {"btree_node_keys": 64}
         t_build = time.perf_counter()
-        ix = gj.make_index(kind, **index_params(args, kind)).construct(None, keys)
+        ix = gj.make_index(kind, **params).construct(None, keys)
         torch.cuda.synchronize()
         t_build = time.perf_counter() - t_build
 
@@ -281,8 +357,16 @@ def inlj_workload(args, world, rank, device, stream):
             clocks = sampler.stop()
         ms = max_over_ranks(ms, world, device)
         got = int(count.item())
-        per_index[kind] = {"tuples_per_s": world * m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
-                           "pairs": got, "build_s": round(t_build, 3), "index_bytes": ix.memory_consumption()}
+        sem = "exact" if kind in EXACT_KINDS else "lower_bound"
+        if kind == "no_op":
+            sem = None
+        parity = None
+        if expect is not None:
+            parity = check_pairs(pairs, count, expect[sem]) if sem else {"checked": m, "mismatches": int(got != 0)}
+        per_index[entry] = {"tuples_per_s": world * m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                            "pairs": got, "build_s": round(t_build, 3), "index_bytes": ix.memory_consumption(),
+                            "params": params or "default build",
+                            "parity": dict(parity, semantics=sem, oracle="all probes") if parity else None}
         if headline_index is None:
             headline_index, headline_ms, headline_ix = kind, ms, ix
         else:
@@ -352,9 +436,8 @@ def inlj_workload(args, world, rank, device, stream):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        h_keys = keys.cpu().numpy().view(np.uint64)
-        hp = probes[: args.cpu_sample].cpu().numpy().view(np.uint64)
-        cpu = cpu_baseline_btree(h_keys, hp, args.cpu_sample)
+        cpu = cpu_baseline_btree(h_keys, h_probes[: args.cpu_sample], args.cpu_sample)
+    parity_all = {k: v["parity"] for k, v in per_index.items() if v.get("parity")}
 
     value = per_index[headline_index]["tuples_per_s"]
     line = {
@@ -376,6 +459,11 @@ def inlj_workload(args, world, rank, device, stream):
                    "output": "(probe row u32, build pos u32) pairs", "l2": "inputs larger than L2 (no flush)",
                    "parallelism": f"replicas x{world}"},
         "per_index": per_index,
+        "parity": {"checked": sum(v["checked"] for v in parity_all.values()),
+                   "mismatches": sum(v["mismatches"] for v in parity_all.values()),
+                   "per_index": {k: v["mismatches"] for k, v in parity_all.items()},
+                   "oracle": "oracle/oracle.c B+tree restatement (lower bound; exact = equal key), every probe",
+                   "oracle_s": round(oracle_s, 2)},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -456,6 +544,11 @@ def partitioned_workload(args, world, rank, device, stream):
     plain_ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, pws), max(2, args.steps // 2), 1, stream, world,
                           device) / max(2, args.steps // 2)
 
+    import numpy as np
+
+    sem = "exact" if kind in EXACT_KINDS else "lower_bound"
+    parity = check_pairs_sample(pairs, count, m, keys.cpu().numpy().view(np.uint64),
+                                probes.cpu().numpy().view(np.uint64), args.parity_sample, args.seed + 7, sem)
     per_step = ms / args.steps
     bpp = 8 + 12 + 12 + 8 + 8.0 * n / m
     peak, peak_kind = measured_peak()
@@ -469,6 +562,7 @@ def partitioned_workload(args, world, rank, device, stream):
         {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune": tune,
                          "plain_pairs_ms_per_step": plain_ms,
                          "plain_pairs_tuples_per_s": m / (plain_ms / 1e3)},
+         "parity": parity,
          "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                       "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_probe": bpp,
                       "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
@@ -680,19 +774,38 @@ def star_workload(args, world, rank, device, stream):
          "gpu_launches": args.steps, "cpu_baseline": None, "e2e": None})
 
 
-def learned_workload(args, world, rank, device, stream):
+def learned_workload(args, world, rank, device, stream, steps=None):
     """Learned index against binary search and RadixSpline at exact outputs:
     2^27 keys from three distributions, 2^28 uniformly sampled probes with 5%
-    absent keys, lower-bound positions."""
+    absent keys, lower-bound positions.  The learned index runs as its
+    default build (column-sized leaves, root chosen per column) and at the
+    configuration's 2^14 leaves (root chosen per column, and the 2x32 MLP
+    root alone); RadixSpline at its default error 32 and at the learned
+    model's recorded error bound.  Every index's positions are compared with
+    the oracle on a seeded sample of probe rows plus every absent key, and
+    in full with the GPU binary search."""
+    import numpy as np
     import torch
 
     import gpujoin_gb300 as gj
 
+    steps = steps or args.steps
     n_log2 = args.n_log2 if args.n_log2 != 26 else 27
     n, m = 1 << n_log2, 1 << args.m_log2
     results = {}
     out = torch.empty(m, dtype=torch.int32, device=device)
     ref = torch.empty(m, dtype=torch.int32, device=device)
+    leaves = {"learned_leaves": args.learned_leaves} if args.learned_leaves else {}
+    configs = (("binary_search", "binary_search", {}), ("radix_spline", "radix_spline", {}),
+               ("learned", "learned", dict(leaves)),
+               ("learned_2^14_leaves", "learned", {"learned_leaves": 1 << 14}),
+               ("learned_mlp_2^14_leaves", "learned", {"learned_root": gj.LEARNED_ROOT_MLP, "learned_leaves": 1 << 14}),
+               ("learned_mlp", "learned", {"learned_root": gj.LEARNED_ROOT_MLP, **leaves}),
+               ("learned_segments", "learned", {"learned_root": gj.LEARNED_ROOT_SEGMENTS, **leaves}),
+               ("learned_linear", "learned", {"learned_root": gj.LEARNED_ROOT_LINEAR, **leaves}))
+    if args.learned_quick:
+        configs = configs[:5]
+    parity_total = {"checked": 0, "mismatches": 0}
     for dist_name, dist in (("uniform", gj.DIST_UNIFORM), ("lognormal", gj.DIST_LOGNORMAL),
                             ("clusters", gj.DIST_CLUSTERS)):
         keys = gj.generate_sorted_keys(n, dist, 1 << 63, seed=args.seed + dist)
@@ -700,44 +813,63 @@ def learned_workload(args, world, rank, device, stream):
         row = {}
         bs = gj.binary_search_index().construct(None, keys)
         bs.lookup(probes, ref)
-        leaves = {"learned_leaves": args.learned_leaves} if args.learned_leaves else {}
-        for kind, kw in (("binary_search", {}), ("radix_spline", {}), ("learned", dict(leaves)),
-                         ("learned_mlp", {"learned_root": gj.LEARNED_ROOT_MLP, **leaves}),
-                         ("learned_segments", {"learned_root": gj.LEARNED_ROOT_SEGMENTS, **leaves}),
-                         ("learned_linear", {"learned_root": gj.LEARNED_ROOT_LINEAR, **leaves})):
+        bs.free()
+        # rows checked against the oracle: a seeded sample plus every absent key
+        present = (ref != -1) & (keys[ref.clamp(min=0).long()] == probes)
+        absent_rows = torch.nonzero(~present).squeeze(1).cpu().numpy()
+        rng = np.random.default_rng(args.seed + 20 + dist)
+        rows = np.union1d(rng.integers(0, m, size=min(args.parity_sample, m)), absent_rows)
+        h_keys = keys.cpu().numpy().view(np.uint64)
+        h_sel = probes[torch.from_numpy(rows).to(device)].cpu().numpy().view(np.uint64)
+        want_lb, _ = oracle_positions(h_keys, h_sel)
+        d_rows = torch.from_numpy(rows).to(device)
+        d_want = torch.from_numpy(want_lb.view(np.int32)).to(device)
+        del h_keys, h_sel
+
+        def judge(entry):
+            bad = int((out[d_rows] != d_want).sum())
+            parity_total["checked"] += len(rows)
+            parity_total["mismatches"] += bad
+            entry["parity"] = {"checked": int(len(rows)), "mismatches": bad, "absent_rows": int(len(absent_rows))}
+            entry["equals_gpu_binary_search"] = bool(torch.equal(out, ref))
+
+        for name, kind, kw in configs:
             t0 = time.perf_counter()
-            ix = gj.make_index(kind.split("_")[0] if kind.startswith("learned") else kind, **kw).construct(None, keys)
+            ix = gj.make_index(kind, **kw).construct(None, keys)
             torch.cuda.synchronize()
             build_s = time.perf_counter() - t0
-            ms = time_steps(lambda: ix.lookup(probes, out), args.steps, args.warmup, stream, world, device)
-            exact = bool(torch.equal(out, ref))
-            entry = {"tuples_per_s": m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "exact": exact,
-                     "build_s": round(build_s, 3), "index_bytes": ix.memory_consumption()}
-            if kind.startswith("learned"):
+            ms = time_steps(lambda: ix.lookup(probes, out), steps, args.warmup, stream, world, device)
+            entry = {"tuples_per_s": m * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "build_s": round(build_s, 3), "index_bytes": ix.memory_consumption(), "params": kw or "default"}
+            judge(entry)
+            if kind == "learned":
                 me, mw = ix.stats()
                 entry.update({"max_error": me, "mean_window": round(mw, 2),
                               "root": ROOT_NAMES[ix.root_kind()]})
-            row[kind] = entry
+            row[name] = entry
             ix.free()
-        # RadixSpline at the learned model's recorded error bound (equal epsilon)
-        eps = int(min(row["learned"]["max_error"], (1 << 31) - 1))
-        ix = gj.radix_spline_index(rs_max_error=max(eps, 1)).construct(None, keys)
-        ms = time_steps(lambda: ix.lookup(probes, out), args.steps, args.warmup, stream, world, device)
-        row["radix_spline_same_eps"] = {"tuples_per_s": m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
-                                        "exact": bool(torch.equal(out, ref)), "max_error": eps,
-                                        "index_bytes": ix.memory_consumption()}
-        ix.free()
-        # the default build (root chosen by the build) against the plain indexes
-        row["learned_beats"] = {k: row["learned"]["tuples_per_s"] > row[k]["tuples_per_s"]
-                                for k in ("binary_search", "radix_spline", "radix_spline_same_eps")}
+        # RadixSpline at the learned models' recorded error bounds (equal epsilon)
+        for lname in ("learned", "learned_2^14_leaves"):
+            eps = int(min(row[lname]["max_error"], (1 << 31) - 1))
+            ix = gj.radix_spline_index(rs_max_error=max(eps, 1)).construct(None, keys)
+            ms = time_steps(lambda: ix.lookup(probes, out), steps, args.warmup, stream, world, device)
+            entry = {"tuples_per_s": m * steps / (ms / 1e3), "ms_per_step": ms / steps, "max_error": eps,
+                     "index_bytes": ix.memory_consumption()}
+            judge(entry)
+            row[f"radix_spline_eps_of_{lname}"] = entry
+            ix.free()
+        for lname in ("learned", "learned_2^14_leaves"):
+            row[f"{lname}_beats"] = {k: row[lname]["tuples_per_s"] > row[k]["tuples_per_s"]
+                                     for k in ("binary_search", "radix_spline", f"radix_spline_eps_of_{lname}")}
         results[dist_name] = row
-        del keys, probes
+        del keys, probes, present, d_rows, d_want
     head = results["uniform"]["learned"]
     return _base_line(
         args, world, "learned-index probe tuples/s (1 GB300 per rank), exact lower bounds",
         world * head["tuples_per_s"], "probe tuples/s", head["ms_per_step"],
         f"learned vs plain: {n} keys (2^{n_log2}) x 3 distributions, {m} probes (2^{args.m_log2}) with 5% absent",
-        {"learned": results, "roofline": None, "gpu_launches": args.steps, "cpu_baseline": None, "e2e": None})
+        {"learned": results, "parity": dict(parity_total, oracle="oracle lower bound on sampled + absent rows"),
+         "roofline": None, "gpu_launches": steps, "cpu_baseline": None, "e2e": None})
 
 
 def batch_workload(args, world, rank, device, stream):
@@ -882,7 +1014,7 @@ def parse_args(argv=None):
     ap.add_argument("--n-log2", type=int, default=26)
     ap.add_argument("--m-log2", type=int, default=28)
     ap.add_argument("--theta", type=float, default=0.5)
-    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned,hash")
+    ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned,hash,btree_w64")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample", type=int, default=1 << 28,
                     help="probes of the CPU baseline leg (one timed pass; about 6 s on 16 Grace cores)")
@@ -895,6 +1027,11 @@ def parse_args(argv=None):
     ap.add_argument("--learned-leaves", type=int, default=0, help="learned: leaf models (0 = library default)")
     ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")
     ap.add_argument("--window", type=int, default=0, help="partitioned: window size in probes (0 = autotune)")
+    ap.add_argument("--parity-sample", type=int, default=1 << 25,
+                    help="probe rows checked against the oracle where not every probe is checked")
+    ap.add_argument("--learned-quick", action="store_true",
+                    help="learned: only binary search, RadixSpline and the learned builds at both leaf counts")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (timing runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     return ap.parse_args(argv)

@@ -135,6 +135,7 @@ _SIGNATURES = {
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_status": (_i32, [_vp, _sz, _u64, _vp]),
+    "gj_debug_inlj_pairs_stalled": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _u32, _vp]),
     "gj_inlj_pairs_host_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
@@ -402,7 +403,19 @@ class abstract_index:
     def inlj_pairs_noalloc(self, d_probes, out_pairs, out_count, stream=None):
         """inlj_pairs without a workspace: the scratch is a fixed array inside the
         library, for callers that cannot allocate while probing (at most
-        2^28 probes per call; overlapping calls must be serialised)."""
+        2^28 probes per call; overlapping calls must be serialised).  The
+        caller's buffers are written in place: out_pairs must hold 2m int32 and
+        out_count one int64, on the probes' device."""
+        torch = _torch()
+        m = d_probes.numel()
+        if out_pairs.dtype != torch.int32 or out_pairs.numel() < 2 * m:
+            raise ValueError(f"inlj_pairs_noalloc: out_pairs must be int32 with at least {2 * m} elements")
+        if out_count.dtype != torch.int64 or out_count.numel() < 1:
+            raise ValueError("inlj_pairs_noalloc: out_count must be int64 with at least one element")
+        if out_pairs.device != d_probes.device or out_count.device != d_probes.device:
+            raise ValueError("inlj_pairs_noalloc: probes, pairs and count must be on the same device")
+        if not (out_pairs.is_contiguous() and out_count.is_contiguous()):
+            raise ValueError("inlj_pairs_noalloc: out_pairs and out_count must be contiguous")
         _check(lib().gj_inlj_pairs_noalloc(self.handle, _ptr(d_probes), d_probes.numel(), _ptr(out_pairs),
                                            _ptr(out_count), _stream(stream)))
         return out_pairs, out_count

@@ -858,6 +858,16 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
                         d_pairs ? d_pairs + m : nullptr, as_stream(stream));
 }
 
+int gj_debug_inlj_pairs_stalled(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                                uint64_t* d_count, void* d_workspace, size_t workspace_bytes, uint32_t spin_limit,
+                                void* stream) {
+    GJ_CHECK_ARG(index && d_count && d_probes && d_pairs, "gj_debug_inlj_pairs_stalled: null argument");
+    GJ_CHECK_ARG(m > 0 && m <= (uint64_t)UINT32_MAX, "gj_debug_inlj_pairs_stalled: m not in [1, 2^32)");
+    GJ_CHECK_ARG(spin_limit > 0, "gj_debug_inlj_pairs_stalled: spin_limit must be > 0");
+    return launch_pairs_stalled(index, d_probes, m, d_pairs, d_count, d_workspace, workspace_bytes, spin_limit,
+                                as_stream(stream));
+}
+
 int gj_index_lookup_sorted(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,
                            void* stream) {
     GJ_CHECK_ARG(index, "gj_index_lookup_sorted: null index");

@@ -149,7 +149,24 @@ int launch_partitioned_pairs(const gj_index* idx, const uint64_t* d_keys, const 
                              uint32_t* d_pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes,
                              cudaStream_t s);
 size_t pairs_workspace_bytes(uint64_t m);
+// launch_pairs for the test of the bounded waits: look-backs give up after
+// spin_limit polls, and tile 0 is never claimed (so every wait runs out)
+int launch_pairs_stalled(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                         uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t spin_limit, cudaStream_t s);
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s);
+
+// range partition of probe keys (gj_partition.cu): partition(k) =
+// min((k - min_key) >> shift, 2^radix_bits - 1), keys <= min_key in 0;
+// d_out_* in partition order, d_offsets (2^radix_bits + 1, optional) the
+// partition starts; rows are row_base + input index
+size_t partition_ws_bytes(uint64_t m, uint32_t radix_bits, int sm_count);
+int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift, uint32_t radix_bits,
+                         uint64_t row_base, uint64_t* d_out_keys, uint32_t* d_out_rows, uint64_t* d_offsets, void* ws,
+                         size_t ws_bytes, cudaStream_t s);
+// fanout for an index of n keys (about 64K keys a partition, 2^8..2^12)
+uint32_t default_radix_bits(uint64_t n);
+// smallest shift that maps [min_key, max_key] onto 2^radix_bits partitions
+uint32_t shift_for(uint64_t min_key, uint64_t max_key, uint32_t radix_bits);
 
 // device-wide inclusive scans over uint64 (gj_gen.cu); workspace scan_workspace_bytes(n)
 size_t scan_workspace_bytes(uint64_t n);

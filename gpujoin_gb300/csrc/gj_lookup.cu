@@ -65,6 +65,15 @@ int launch_partitioned_pairs(const gj_index* idx, const uint64_t* d_keys, const 
                           nullptr, s});
 }
 
+int launch_pairs_stalled(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                         uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t spin_limit, cudaStream_t s) {
+    lookup_call c{lookup_action::pairs, d_probes, nullptr, m, d_pairs, nullptr, d_count, ws, ws_bytes,
+                  d_pairs ? d_pairs + m : nullptr, s};
+    c.spin_limit = spin_limit;
+    c.skip_first_tile = true;
+    return dispatch(idx, c);
+}
+
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s) {
     pairs_ws pw;
     size_t used = 0;

@@ -38,6 +38,11 @@ struct lookup_call {
     size_t ws_bytes;
     uint32_t* stash;       // pairs: two-pass positions buffer, or null
     cudaStream_t s;
+    // test hook of the bounded waits (gj_debug_inlj_pairs_stalled): a spin
+    // limit other than kSpinLimit (0 = default) and a first tile left
+    // unclaimed, so that every look-back runs out
+    uint32_t spin_limit;
+    bool skip_first_tile;
 };
 
 // per-kind entry points, each defined in one unit
@@ -270,6 +275,7 @@ struct pairs_ws {
     unsigned long long* tile_state;  // num_tiles
     unsigned int* tile_counter;      // 1
     unsigned int* error;             // 1
+    uint32_t spin_limit;             // polls before a look-back gives up
 };
 
 // the workspace layout of every pairs kernel; false when it is too small
@@ -279,6 +285,7 @@ inline bool carve_pairs_ws(void* ws, size_t ws_bytes, uint64_t m, pairs_ws* pw, 
     pw->tile_state = wc.take<unsigned long long>(states ? states : 1);
     pw->tile_counter = wc.take<unsigned int>(2);
     pw->error = pw->tile_counter ? pw->tile_counter + 1 : nullptr;
+    pw->spin_limit = kSpinLimit;
     *used = wc.used;
     return pw->tile_state && pw->tile_counter;
 }
@@ -302,7 +309,7 @@ __device__ __forceinline__ bool look_back(const pairs_ws& ws, uint32_t tile, uin
         // lanes up to (and including) the nearest prefix must all be published
         const uint32_t need = has_prefix ? (2u << (__ffs(has_prefix) - 1)) - 1u : 0xffffffffu;
         if (not_ready & need) {
-            if (++spins > kSpinLimit) return false;
+            if (++spins > ws.spin_limit) return false;
             continue;
         }
         unsigned long long v = ((need >> lane) & 1u) ? (st & kValueMask) : 0ull;
@@ -785,7 +792,7 @@ int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const 
 template <class Op>
 int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const uint32_t* rows, uint64_t m,
               uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* stash,
-              cudaStream_t s) {
+              cudaStream_t s, uint32_t spin_limit = 0, bool skip_first_tile = false) {
     const uint32_t num_tiles = (uint32_t)((m + kTile - 1) / kTile);
     pairs_ws pw;
     size_t used = 0;
@@ -802,6 +809,10 @@ int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const 
         return GJ_OK;
     }
     GJ_CUDA_TRY(cudaMemsetAsync(ws, 0, used, s));
+    if (spin_limit) pw.spin_limit = spin_limit;
+    // test hook: the tile counter starts at 1, so tile 0 is never claimed and
+    // never publishes; every later tile's look-back runs out
+    if (skip_first_tile) GJ_CUDA_TRY(cudaMemsetAsync(pw.tile_counter, 1, 1, s));
     if (stash) {
         GJ_TRY(run_lookup(op, sd, probes, m, stash, s));
         const uint32_t compact_tiles = (uint32_t)((m + kCompactTile - 1) / kCompactTile);
@@ -863,7 +874,8 @@ int run_call(const Op& op, const gj_index* idx, const lookup_call& c) {
         case lookup_action::positions: return run_lookup(op, sd, c.keys, c.m, c.out, c.s);
         case lookup_action::scatter: return run_scatter(op, sd, c.keys, c.rows, c.m, c.out, c.s);
         case lookup_action::pairs:
-            return run_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.stash, c.s);
+            return run_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.stash, c.s,
+                             c.spin_limit, c.skip_first_tile);
         case lookup_action::sorted_pairs:
             return run_sorted_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.s);
         case lookup_action::sorted_positions: return run_sorted_lookup(op, sd, c.keys, c.m, c.out, c.s);

@@ -1,20 +1,19 @@
-// gj_partition.cu -- range partitioning of the probe side and the windowed
-// partitioned INLJ.
+// gj_partition.cu -- range partitioning of the probe side.
 //
 // Replaces the fast-interconnects prefix-sum + chunked radix-partition
-// kernels driven by run_on_stream (src/index_lookup_partitioning.cu:300-359)
-// and the window loop of partitioning_approach (:436-507).  The reference
+// kernels driven by run_on_stream (src/index_lookup_partitioning.cu:300-359).
+// The reference
 // partitions on key bits [max_bits - 11, max_bits) (src/index_lookup_new.cu:
 // 63-67); here the partition function is a range split of the index's key
 // range, partition(k) = min((k - min) >> shift, fanout - 1), so each partition
 // maps onto one contiguous slice of the index and a window's lookups walk the
 // index in order (the slices stay resident in the 126 MB L2).
 //
-// Pipeline per window (all on the caller's stream):
-//   1. k_part_hist   per-block histograms of the window's keys
+// A partition pass (all on the caller's stream):
+//   1. k_part_hist   per-block histograms of the keys
 //   2. scan          exclusive offsets, partition-major (p, block)
 //   3. k_part_scatter keys and row ids to their partition, in block order
-//   4. lookup        scattered positions and/or pairs in partition order
+// The windowed partitioned INLJ that drives it is in gj_partitioned.cu.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -205,15 +204,107 @@ size_t scatter_smem_bytes(uint32_t fanout) {
     return (size_t)kScatterTile * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)fanout * (8 + 4 + 4);
 }
 
+// The scatter for fanouts of 2^9 and more: the same counting sort per tile,
+// with tiles large enough that a partition's run in a tile still covers
+// whole sectors (8192 keys: 8 a partition at 2^10, 2 at 2^12), one
+// 1024-thread block per SM, and the next tile's keys loaded into registers
+// while the current tile is sorted and written.  A key's place in the tile
+// is kept as a 16-bit offset (its row is row_base + tile start + offset).
+constexpr uint32_t kWideRadixBits = 9;
+constexpr int kWideBlock = 1024;
+constexpr int kWideItems = 8;
+constexpr uint32_t kWideTile = kWideBlock * kWideItems;
+
+__global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint64_t* __restrict__ keys, uint64_t m,
+                                                                     uint64_t chunk, uint64_t min_key, uint32_t shift,
+                                                                     uint32_t fanout, const uint64_t* __restrict__ incl,
+                                                                     uint64_t row_base, uint64_t* __restrict__ out_keys,
+                                                                     uint32_t* __restrict__ out_rows) {
+    extern __shared__ unsigned long long s_mem[];
+    uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_mem);             // kWideTile
+    unsigned long long* s_dst = s_mem + kWideTile;                     // fanout: next output slot
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_dst + fanout);     // fanout
+    uint32_t* s_start = s_cnt + fanout;                                // fanout
+    uint16_t* s_off = reinterpret_cast<uint16_t*>(s_start + fanout);   // kWideTile
+    for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) {
+        const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
+        s_dst[p] = cell == 0 ? 0ull : incl[cell - 1];
+        s_cnt[p] = 0;
+    }
+    const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
+    const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
+    static_assert(kWideTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
+    static_assert(kWideTile <= (1u << 16), "16-bit tile offsets");
+    uint64_t next[kWideItems];
+#pragma unroll
+    for (int k = 0; k < kWideItems; ++k) {
+        const uint64_t i = b0 + (uint64_t)k * kWideBlock + threadIdx.x;
+        next[k] = i < b1 ? __ldcs(k64 + i) : 0ull;
+    }
+    __syncthreads();
+    for (uint64_t t0 = b0; t0 < b1; t0 += kWideTile) {
+        const uint32_t tn = b1 - t0 < kWideTile ? (uint32_t)(b1 - t0) : kWideTile;
+        uint64_t key[kWideItems];
+#pragma unroll
+        for (int k = 0; k < kWideItems; ++k) key[k] = next[k];
+        const uint64_t t1 = t0 + kWideTile;
+#pragma unroll
+        for (int k = 0; k < kWideItems; ++k) {
+            const uint64_t i = t1 + (uint64_t)k * kWideBlock + threadIdx.x;
+            next[k] = i < b1 ? __ldcs(k64 + i) : 0ull;
+        }
+        uint32_t slot[kWideItems];  // partition << 13 | rank inside the tile's partition run
+#pragma unroll
+        for (int k = 0; k < kWideItems; ++k) {
+            const uint32_t j = k * kWideBlock + threadIdx.x;
+            const uint32_t p = part_of(key[k], min_key, shift, fanout);
+            slot[k] = j < tn ? (p << 13) | atomicAdd(&s_cnt[p], 1u) : 0u;
+        }
+        __syncthreads();
+        block_exclusive_scan<kWideBlock>(s_cnt, s_start, fanout);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kWideItems; ++k) {
+            const uint32_t j = k * kWideBlock + threadIdx.x;
+            if (j < tn) {
+                const uint32_t q = s_start[slot[k] >> 13] + (slot[k] & ((1u << 13) - 1));
+                s_keys[q] = key[k];
+                s_off[q] = (uint16_t)j;
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < tn; j += kWideBlock) {
+            const uint64_t k = s_keys[j];
+            const uint32_t p = part_of(k, min_key, shift, fanout);
+            const uint64_t d = s_dst[p] + (j - s_start[p]);
+            __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
+            __stcg(out_rows + d, (uint32_t)(row_base + t0 + s_off[j]));
+        }
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) {
+            s_dst[p] += s_cnt[p];
+            s_cnt[p] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+size_t scatter_wide_smem_bytes(uint32_t fanout) {
+    return (size_t)kWideTile * (sizeof(uint64_t) + sizeof(uint16_t)) + (size_t)fanout * (8 + 4 + 4);
+}
+
 struct partition_plan {
     uint32_t fanout, nblocks;
     uint64_t chunk;
+    bool wide;
 };
 
 partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
     partition_plan pl;
     pl.fanout = 1u << radix_bits;
-    uint64_t nb = (uint64_t)sm_count * kScatterPerSM;  // the scatter kernel's resident blocks
+    pl.wide = radix_bits >= kWideRadixBits;
+    // the scatter kernel's resident blocks
+    uint64_t nb = (uint64_t)sm_count * (pl.wide ? 1 : kScatterPerSM);
     const uint64_t min_chunk = 4096;
     if (nb * min_chunk > m) nb = std::max<uint64_t>(1, (m + min_chunk - 1) / min_chunk);
     pl.chunk = (m + nb - 1) / nb;
@@ -221,6 +312,8 @@ partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
     if (pl.nblocks == 0) pl.nblocks = 1;
     return pl;
 }
+
+}  // namespace
 
 size_t partition_ws_bytes(uint64_t m, uint32_t radix_bits, int sm_count) {
     const partition_plan pl = plan_partition(m ? m : 1, radix_bits, sm_count);
@@ -248,9 +341,15 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
         return GJ_OK;
     }
     const size_t smem_hist = (size_t)pl.fanout * hist_copies(pl.fanout) * sizeof(uint32_t);
-    const size_t smem_scatter = scatter_smem_bytes(pl.fanout);
-    if (smem_scatter > 48 * 1024)
-        GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_scatter));
+    const size_t smem_scatter = pl.wide ? scatter_wide_smem_bytes(pl.fanout) : scatter_smem_bytes(pl.fanout);
+    if (smem_scatter > 48 * 1024) {
+        if (pl.wide)
+            GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem_scatter));
+        else
+            GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem_scatter));
+    }
     k_part_hist<<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
     GJ_CUDA_TRY(cudaGetLastError());
     GJ_TRY(inclusive_scan_sum(hist, cells, scan_ws, scan_workspace_bytes(cells), s));
@@ -258,8 +357,12 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
         k_part_offsets<<<(pl.fanout + 256) / 256, 256, 0, s>>>(hist, pl.fanout, pl.nblocks, m, d_offsets);
         GJ_CUDA_TRY(cudaGetLastError());
     }
-    k_part_scatter<<<pl.nblocks, kScatterBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist,
-                                                                row_base, d_out_keys, d_out_rows);
+    if (pl.wide)
+        k_part_scatter_wide<<<pl.nblocks, kWideBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout,
+                                                                         hist, row_base, d_out_keys, d_out_rows);
+    else
+        k_part_scatter<<<pl.nblocks, kScatterBlock, smem_scatter, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout,
+                                                                    hist, row_base, d_out_keys, d_out_rows);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
 }
@@ -283,7 +386,6 @@ uint32_t shift_for(uint64_t min_key, uint64_t max_key, uint32_t radix_bits) {
     return used > radix_bits ? used - radix_bits : 0u;
 }
 
-}  // namespace
 }  // namespace gj
 
 using namespace gj;
@@ -318,72 +420,6 @@ int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, co
     GJ_CHECK_ARG(index, "gj_partitioned_lookup: null index");
     GJ_CHECK_ARG(m == 0 || (d_part_keys && d_part_rows && d_positions), "gj_partitioned_lookup: null buffer");
     return launch_scatter_lookup(index, d_part_keys, d_part_rows, m, d_positions, as_stream(stream));
-}
-
-static uint64_t clamp_window(uint64_t m, uint64_t window) {
-    if (window == 0 || window > m) window = m;
-    return window ? window : 1;
-}
-
-int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
-                                       size_t* bytes) {
-    GJ_CHECK_ARG(index && bytes, "gj_partitioned_inlj_workspace_size: null argument");
-    GJ_CHECK_ARG(window_size > 0, "gj_partitioned_inlj_workspace_size: window_size must be > 0");
-    if (radix_bits == 0) radix_bits = default_radix_bits(index->n);
-    GJ_CHECK_ARG(radix_bits <= kMaxRadixBits, "gj_partitioned_inlj_workspace_size: radix_bits > 12");
-    device_info di;
-    GJ_TRY(current_device_info(&di));
-    const uint64_t w = window_size;
-    *bytes = workspace_carver::need({w * sizeof(uint64_t), w * sizeof(uint32_t),
-                                     partition_ws_bytes(w, radix_bits, di.sm_count), pairs_workspace_bytes(w)});
-    return GJ_OK;
-}
-
-int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint64_t window_size,
-                        uint32_t radix_bits, uint32_t* d_positions, uint32_t* d_pairs, uint64_t* d_count,
-                        void* d_workspace, size_t workspace_bytes, void* stream) {
-    GJ_CHECK_ARG(index, "gj_partitioned_inlj: null index");
-    GJ_CHECK_ARG(d_positions || d_pairs, "gj_partitioned_inlj: no output requested");
-    GJ_CHECK_ARG(!d_pairs || d_count, "gj_partitioned_inlj: d_count is required with d_pairs");
-    GJ_CHECK_ARG(m == 0 || d_probes, "gj_partitioned_inlj: null probes");
-    GJ_CHECK_ARG(window_size > 0, "gj_partitioned_inlj: window_size must be > 0");
-    if (m > (uint64_t)UINT32_MAX) {
-        set_error("gj_partitioned_inlj: probe rows must fit 32 bits");
-        return GJ_ERR_TOO_LARGE;
-    }
-    if (radix_bits == 0) radix_bits = default_radix_bits(index->n);
-    GJ_CHECK_ARG(radix_bits <= kMaxRadixBits, "gj_partitioned_inlj: radix_bits > 12");
-    cudaStream_t s = as_stream(stream);
-    device_info di;
-    GJ_TRY(current_device_info(&di));
-    const uint64_t w = window_size;
-    workspace_carver wc(d_workspace, workspace_bytes);
-    uint64_t* pkeys = wc.take<uint64_t>(w);
-    uint32_t* prows = wc.take<uint32_t>(w);
-    const size_t pws_bytes = partition_ws_bytes(w, radix_bits, di.sm_count);
-    void* pws = wc.take<char>(pws_bytes);
-    const size_t qws_bytes = pairs_workspace_bytes(w);
-    void* qws = wc.take<char>(qws_bytes);
-    if (!pkeys || !prows || !pws || !qws) {
-        size_t need = 0;
-        gj_partitioned_inlj_workspace_size(index, window_size, radix_bits, &need);
-        set_error("gj_partitioned_inlj: workspace of %zu bytes is smaller than the %zu required", workspace_bytes, need);
-        return GJ_ERR_WORKSPACE;
-    }
-    if (d_pairs) GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
-    if (m == 0) return GJ_OK;
-    uint64_t min_key = 0, max_key = 0;
-    index_key_range(index, &min_key, &max_key);
-    const uint32_t shift = shift_for(min_key, max_key, radix_bits);
-    for (uint64_t off = 0; off < m; off += w) {
-        const uint64_t len = std::min<uint64_t>(w, m - off);
-        GJ_TRY(range_partition_impl(d_probes + off, len, min_key, shift, radix_bits, off, pkeys, prows, nullptr, pws,
-                                    pws_bytes, s));
-        if (d_positions) GJ_TRY(launch_scatter_lookup(index, pkeys, prows, len, d_positions, s));
-        if (d_pairs)
-            GJ_TRY(launch_partitioned_pairs(index, pkeys, prows, len, d_pairs, d_count, d_count, qws, qws_bytes, s));
-    }
-    return GJ_OK;
 }
 
 }  // extern "C"

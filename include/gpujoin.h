@@ -214,6 +214,16 @@ int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t
  * reference, whose compaction does not wait. */
 int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream);
 
+/* Test hook of the bounded waits, with no counterpart in the reference: runs
+ * gj_inlj_pairs with the first tile left unclaimed and a look-back limit of
+ * spin_limit polls, so every later tile's wait runs out and the kernel
+ * returns with the error word set (gj_inlj_pairs_status then returns
+ * GJ_ERR_TIMEOUT; *d_count is not written).  Nothing faults or hangs: the
+ * waits are bounded and every block exits. */
+int gj_debug_inlj_pairs_stalled(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                                uint64_t* d_count, void* d_workspace, size_t workspace_bytes,
+                                uint32_t spin_limit, void* stream);
+
 /* Same pairs as gj_inlj_pairs, for callers that cannot allocate device
  * memory when they probe (a frozen allocator, someone else's memory arena,
  * or a probe path that must not call cudaMalloc/cudaFree because they
@@ -222,9 +232,21 @@ int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64
  * library, held until the process exits), so it needs no workspace argument
  * and allocates nothing.  At most GJ_NOALLOC_MAX_PROBES probes per call;
  * larger m returns GJ_ERR_TOO_LARGE.  The first call on a device looks up the
- * array's device address: make it before capturing a stream.  All calls
+ * array's device address; under lazy module loading that lookup may also
+ * load the library's device code and back the array, i.e. allocate and
+ * synchronise once.  So warm it up at start-up: make one call per device
+ * (m = 0 is enough) before the probe path runs and before capturing a
+ * stream.  The address is kept per device ordinal and is valid in the
+ * device's primary context only (the runtime API's default).  All calls
  * share the array: calls whose kernels overlap on the GPU (other streams,
- * other host threads) must be serialised by the caller. */
+ * other host threads) must be serialised by the caller.
+ * A bounded device wait that gives up is NOT reported on this path: the
+ * error word lives in the library's array, which gj_inlj_pairs_status
+ * cannot see, and the next call clears it.  The wait only gives up when a
+ * predecessor tile makes no progress for about 2^22 polls (seconds), which
+ * the kernel's in-order tile claims rule out short of a GPU preemption of
+ * that length; a caller that must detect it uses gj_inlj_pairs with its own
+ * workspace and gj_inlj_pairs_status. */
 #define GJ_NOALLOC_MAX_PROBES (1ull << 28)
 int gj_inlj_pairs_noalloc(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                           uint64_t* d_count, void* stream);
@@ -249,11 +271,15 @@ int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, co
 /* The windowed partitioned INLJ (partitioning_approach::run,
  * src/index_lookup_partitioning.cu:436-507): the probe column is cut into
  * windows of window_size probes; each window is range-partitioned on the
- * index's key range and probed partition by partition.  Emits d_positions
- * in probe order (equal to gj_index_lookup) when d_positions != NULL, and/or
- * (row, pos) pairs of the matches in partition order when d_pairs != NULL
- * (*d_count = number of pairs).  radix_bits = 0 picks the fanout from the
- * index size.  Workspace: gj_partitioned_inlj_workspace_size. */
+ * index's key range and every partition is probed against its slice of the
+ * index's column through a partition directory built once per call (each
+ * index kind's result semantics kept).  Emits d_positions in probe order
+ * (equal to gj_index_lookup) when d_positions != NULL, and/or the (row, pos)
+ * pairs of the matches when d_pairs != NULL (*d_count = number of pairs);
+ * the set of pairs is fixed, their order is not (tiles of a window append
+ * in the order they finish, as the reference's atomics do,
+ * src/tpch/tpch_14_ij.cu:371-407).  radix_bits = 0 picks the fanout from
+ * the index size.  Workspace: gj_partitioned_inlj_workspace_size. */
 int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
                                        size_t* bytes);
 int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint64_t window_size,

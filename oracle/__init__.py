@@ -68,6 +68,8 @@ def lib() -> ctypes.CDLL:
         L.orc_btree_build.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
         L.orc_btree_lookup.restype = None
         L.orc_btree_lookup.argtypes = [_vp, _u64p, ctypes.c_uint64, _u32p, ctypes.c_int]
+        L.orc_btree_lower_bound.restype = None
+        L.orc_btree_lower_bound.argtypes = [_vp, _u64p, ctypes.c_uint64, _u32p, ctypes.c_int]
         L.orc_btree_depth.restype = ctypes.c_uint32
         L.orc_btree_depth.argtypes = [_vp]
         L.orc_btree_free.argtypes = [_vp]
@@ -190,6 +192,13 @@ class BTree:
         lib().orc_btree_lookup(self._h, _ptr(probes, _u64p), len(probes), _ptr(out, _u32p), threads)
         return out
 
+    def lower_bound(self, probes, threads: int = 0) -> np.ndarray:
+        """bs_lookup's results (first key >= probe, INV at n) through the tree."""
+        probes = _u64(probes)
+        out = np.empty(len(probes), dtype=np.uint32)
+        lib().orc_btree_lower_bound(self._h, _ptr(probes, _u64p), len(probes), _ptr(out, _u32p), threads)
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib().orc_btree_free(self._h)
@@ -274,6 +283,18 @@ def range_partition(keys, min_key: int, shift: int, radix_bits: int):
     lib().orc_range_partition(_ptr(keys, _u64p), m, int(min_key), shift, radix_bits, _ptr(ok, _u64p),
                               _ptr(orows, _u32p), _ptr(offsets, _u64p))
     return ok, orows, offsets
+
+
+def fast_positions(col, probes, threads: int = 0) -> Tuple[np.ndarray, np.ndarray]:
+    """(lower bound, exact) positions of every probe for large checks: the
+    lower bound (bs_lookup's semantics) through the oracle B+tree, and the
+    exact-match form (B+tree / Harmonia / hash semantics) derived from it."""
+    col, probes = _u64(col), _u64(probes)
+    lb = BTree(col, 247, 246).lower_bound(probes, threads)
+    ok = lb != INV
+    hit = np.zeros(len(probes), dtype=bool)
+    hit[ok] = col[lb[ok]] == probes[ok]
+    return lb, np.where(hit, lb, np.uint32(INV)).astype(np.uint32)
 
 
 def pairs_from_positions(pos) -> Tuple[np.ndarray, np.ndarray]:

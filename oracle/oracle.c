@@ -271,6 +271,34 @@ void orc_btree_lookup(const orc_btree* t, const uint64_t* probes, uint64_t m, ui
     orc_parallel_for(m, threads, bt_range, &c);
 }
 
+/* The global lower bound through the same tree (binary_search_index's
+ * semantics, src/indexes.cuh:357-361: position of the first key >= probe,
+ * ORC_INV at n).  Separators are the children's maximum keys, so the lower
+ * bound over a node's separators names the child holding the lower bound;
+ * only the rightmost leaf can come up empty (probe above every key).  A
+ * faster restatement of orc_bs_lookup for large checks (tests compare the
+ * two). */
+static uint32_t bt_lower_bound_one(const orc_btree* t, uint64_t key) {
+    uint64_t ref = t->root;
+    for (;;) {
+        const orc_bnode* nd = &t->nodes[ref];
+        uint64_t pos = orc_branchy_binary_search(nd->keys, nd->count, key);
+        ref = nd->children[pos];
+        if (nd->is_final_inner) break;
+    }
+    uint64_t cnt = t->n - ref < t->leaf_keys ? t->n - ref : t->leaf_keys;
+    uint64_t lb = ref + orc_branchy_binary_search(t->col + ref, cnt, key);
+    return lb < t->n ? (uint32_t)lb : ORC_INV;
+}
+static void bt_lb_range(void* p, uint64_t b, uint64_t e) {
+    bt_ctx* c = (bt_ctx*)p;
+    for (uint64_t i = b; i < e; ++i) c->out[i] = bt_lower_bound_one(c->t, c->probes[i]);
+}
+void orc_btree_lower_bound(const orc_btree* t, const uint64_t* probes, uint64_t m, uint32_t* out, int threads) {
+    bt_ctx c = {t, probes, out};
+    orc_parallel_for(m, threads, bt_lb_range, &c);
+}
+
 void orc_btree_free(orc_btree* t) {
     if (!t) return;
     for (uint64_t i = 0; i < t->nnodes; ++i) { free(t->nodes[i].keys); free(t->nodes[i].children); }

@@ -50,6 +50,8 @@ orc_btree* orc_btree_build(const uint64_t* col, uint64_t n, uint32_t leaf_keys,
                            uint32_t inner_keys);
 void orc_btree_lookup(const orc_btree* t, const uint64_t* probes, uint64_t m,
                       uint32_t* out, int threads);
+/* lower bound (INV at n) through the same tree: orc_bs_lookup's results, faster */
+void orc_btree_lower_bound(const orc_btree* t, const uint64_t* probes, uint64_t m, uint32_t* out, int threads);
 uint32_t orc_btree_depth(const orc_btree* t);
 void orc_btree_free(orc_btree* t);
 

@@ -1,0 +1,61 @@
+"""The partitioned INLJ's partition directory on the columns that stress it,
+against the oracle: a partition whose column slice is too wide for 16-bit
+directory offsets (searched over its whole slice), a column that is not
+32-byte aligned, columns of a few keys, clustered keys with long gaps
+(directory entries filled by the fill pass), probes outside the key range,
+and several windows.  Positions must equal the oracle's per probe row, the
+pairs as a set (their order across tiles is not fixed)."""
+import numpy as np
+import pytest
+
+from test_lookup_gpu import column, expected, from_dev_u32, probes_for, to_dev
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["btree", "binary_search", "radix_spline", "hash", "learned", "no_op"]
+
+
+def _column(case, rng):
+    if case == "wide":
+        # 2^19 dense keys in partition 0 (2^17 sectors: too wide for the
+        # directory) and 2^19 keys spread over the rest of the range
+        dense = np.arange(1000, 1000 + (1 << 19), dtype=np.uint64)
+        sparse = np.unique(rng.integers(1 << 40, 1 << 63, size=(1 << 19) + 4096, dtype=np.uint64))[: 1 << 19]
+        return np.concatenate([dense, sparse])
+    if case == "clusters":
+        starts = np.sort(rng.choice(1 << 50, size=64, replace=False).astype(np.uint64)) << np.uint64(10)
+        col = np.concatenate([s + np.arange(4096, dtype=np.uint64) * np.uint64(3) for s in starts])
+        return np.unique(col)
+    if case == "tiny":
+        return np.array([5, 17, 1 << 40, (1 << 64) - 2, (1 << 64) - 1], dtype=np.uint64)
+    return column(rng, 100_003)  # "unaligned" and "plain"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("case", ["wide", "unaligned", "tiny", "clusters"])
+def test_partitioned_directory_cases(orc, gj, cuda, kind, case):
+    import torch
+
+    rng = np.random.default_rng(len(case) * 31 + len(kind))
+    col = _column(case, rng)
+    pr = probes_for(rng, col, 60_000)
+    if case == "unaligned":
+        d_all = to_dev(torch, np.concatenate([np.array([0], dtype=np.uint64), col]))
+        d_col = d_all[1:]  # 8-byte offset: not 32-byte aligned
+        assert d_col.data_ptr() % 32 != 0
+    else:
+        d_col = to_dev(torch, col)
+    ix = gj.make_index(kind).construct(None, d_col)
+    exp = expected(orc, kind, col, pr)
+    erows, epos = orc.pairs_from_positions(exp)
+    for bits, window in ((8, 0), (12, 0), (10, 7777)):
+        pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=bits, positions=True,
+                                            pairs=True)
+        got = from_dev_u32(pos)
+        bad = np.nonzero(got != exp)[0]
+        assert len(bad) == 0, f"{kind}/{case}/2^{bits}: {len(bad)} positions differ, rows {bad[:5]}"
+        c = int(cnt.item())
+        a = prs[: 2 * c].cpu().numpy().view(np.uint32).reshape(-1, 2)
+        order = np.argsort(a[:, 0], kind="stable")
+        np.testing.assert_array_equal(a[order, 0], erows, err_msg=f"{kind}/{case}/2^{bits}")
+        np.testing.assert_array_equal(a[order, 1], epos, err_msg=f"{kind}/{case}/2^{bits}")
