@@ -299,6 +299,151 @@ def gpu_main(args):
         print(json.dumps(line), flush=True)
 
 
+def random_sector_rate(device, stream, n_sectors=1 << 26, loads=1 << 28, reps=5):
+    """Random 32-byte sector reads per second over a 2 GiB buffer (larger than
+    L2), CUDA events, best of reps, with the default L2 fill and with the
+    64-byte fill the probe kernels' scattered loads ask for
+    (gj_calibrate_random_sectors)."""
+    import ctypes
+
+    import torch
+
+    import gpujoin_gb300 as gj
+
+    buf = torch.randint(0, 1 << 62, (4 * n_sectors,), dtype=torch.int64, device=device)
+    words = ctypes.c_uint64(0)
+    gj._check(gj.lib().gj_calibrate_sink_words(ctypes.byref(words)))
+    sink = torch.empty(words.value, dtype=torch.int64, device=device)
+    out = {"buffer_bytes": 32 * n_sectors, "loads": loads}
+    for fill64, name in ((0, "default_fill"), (1, "fill_64B")):
+        best = None
+        for r in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gj._check(gj.lib().gj_calibrate_random_sectors(buf.data_ptr(), n_sectors, loads, 12345 + r, fill64,
+                                                          sink.data_ptr(), stream.cuda_stream))
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b)
+            if r and (best is None or t < best):
+                best = t
+        out[name] = {"sectors_per_s": loads / (best / 1e3), "ms": round(best, 3)}
+    del buf, sink
+    torch.cuda.empty_cache()
+    return out
+
+
+def cpu_baselines(h_keys, h_probes, one_sample, all_sample):
+    """The reference's CPU lookup paths (restated in oracle/oracle.c, pinned
+    to the reference's own headers by the golden fixtures) on the host cores:
+    std::lower_bound (binary_search_index's semantics), the branch-free lower
+    bound (src/bf_search.cpp:34-47), Harmonia's host lookup
+    (src/harmonia.cuh:640-668) and the clustered B+tree with the reference's
+    page geometry -- each at 1 thread (as the reference runs them,
+    src/tpch/cpu_bench.cpp:31,37) and at all host threads, on bounded samples
+    of the same probes."""
+    import oracle
+
+    threads = oracle.hardware_threads()
+    bt = oracle.BTree(h_keys, 247, 246)
+    hm = oracle.Harmonia(h_keys)
+    methods = (("lower_bound", lambda pr, t: oracle.bs_lookup(h_keys, pr, t)),
+               ("branch_free_lower_bound", lambda pr, t: oracle.bs_lookup(h_keys, pr, t, branch_free=True)),
+               ("harmonia", lambda pr, t: hm.lookup(pr, t)),
+               ("btree", lambda pr, t: bt.lookup(pr, t)))
+    out = {"cores": threads, "kind": "port", "unit": "probe tuples/s"}
+    for name, f in methods:
+        row = {}
+        for t, sample in ((1, one_sample), (threads, all_sample)):
+            pr = h_probes[:sample]
+            f(pr[:4096], t)  # warm
+            t0 = time.perf_counter()
+            f(pr, t)
+            dt = time.perf_counter() - t0
+            row[f"threads_{t}"] = {"value": len(pr) / dt, "probes": int(len(pr)), "seconds": round(dt, 3)}
+        out[name] = row
+    return out
+
+
+def north_star_extras(args, world, device, stream, keys, h_keys, h_probes):
+    """The other configurations of the INLJ measurement, each checked against
+    the oracle: the same B+tree at Zipf theta 0 and 1.0; the partitioned INLJ
+    of 2^29 Zipf(0.5) probes into a 2^28-key index (autotuned fanout); the
+    learned index against binary search and RadixSpline (2^27 keys x three
+    distributions, 2^28 probes with 5% absent keys); the star-join aggregate;
+    and the reference's CPU lookup paths at 1 and all host threads."""
+    import numpy as np
+    import torch
+
+    import gpujoin_gb300 as gj
+    import oracle
+
+    extras = {}
+    n, m = keys.numel(), h_probes.shape[0]
+    steps = max(3, min(args.steps, args.extra_steps))
+
+    t0 = time.perf_counter()
+    per_theta = {}
+    ix = gj.btree_index().construct(None, keys)
+    pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device)
+    import ctypes
+
+    wsz = ctypes.c_size_t(0)
+    gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(wsz))
+    ws = torch.empty(wsz.value, dtype=torch.uint8, device=device)
+    for theta in (0.0, 1.0):
+        probes = gj.generate_probes(keys, m, theta=theta, seed=args.seed + 1)
+        ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, ws), steps, args.warmup, stream, world, device)
+        parity = None
+        if not args.no_parity:
+            parity = check_pairs_sample(pairs, count, m, h_keys, probes.cpu().numpy().view(np.uint64),
+                                        args.parity_sample, args.seed + 9, "exact")
+        per_theta[str(theta)] = {"tuples_per_s": m * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                                 "pairs": int(count.item()), "parity": parity}
+        del probes
+    ix.free()
+    del pairs, ws
+    torch.cuda.empty_cache()
+    extras["per_theta"] = dict(per_theta, index="btree (default build)", theta_0_5="the headline",
+                               seconds=round(time.perf_counter() - t0, 1))
+
+    t0 = time.perf_counter()
+    extras["partitioned"] = partitioned_measure(args, world, device, stream, 28, 29, steps, "btree")
+    extras["partitioned"]["seconds"] = round(time.perf_counter() - t0, 1)
+
+    t0 = time.perf_counter()
+    results, parity = learned_measure(args, world, device, stream, 27, 28, 3, quick=True)
+    extras["learned"] = {"results": results, "parity": parity, "seconds": round(time.perf_counter() - t0, 1),
+                         "config": "2^27 keys x {uniform, lognormal(0,2) x 2^60, 1024 clusters}, 2^28 probes "
+                                   "(5% absent), 3 timed steps each"}
+
+    t0 = time.perf_counter()
+    n_fact, n_dim, lo, hi = 6_000_000, 200_000, 1000, 1030
+    dim_keys, flag, fk, date, price, disc = star_inputs(n_fact, n_dim, args.seed, device)
+    six = gj.btree_index().construct(None, dim_keys)
+    sout = torch.zeros(2, dtype=torch.int64, device=device)
+    ms = time_steps(lambda: gj.star_join_sum(six, fk, date, price, disc, flag, lo, hi, sout), steps, args.warmup,
+                    stream, world, device)
+    got = sout.cpu().numpy()
+    h = [t.cpu().numpy() for t in (fk, date, price, disc, dim_keys, flag)]
+    c0 = time.perf_counter()
+    num, den = oracle.star_join(h[0].view(np.uint32), h[1].view(np.uint32), h[2], h[3], h[4].view(np.uint64), h[5],
+                                lo, hi)
+    cpu_s = time.perf_counter() - c0
+    extras["star"] = {"fact_rows_per_s": n_fact * steps / (ms / 1e3), "latency_us": ms / steps * 1e3,
+                      "sums": [int(got[0]), int(got[1])], "oracle_sums": [num, den],
+                      "exact": bool(int(got[0]) == num and int(got[1]) == den),
+                      "cpu_query_14_part_build_1_thread_rows_per_s": n_fact / cpu_s,
+                      "config": "6M fact rows, 200k dimension rows (B+tree), 30-day window of 2556 days"}
+    six.free()
+
+    t0 = time.perf_counter()
+    extras["cpu_baselines"] = cpu_baselines(h_keys, h_probes, args.cpu_one_sample, args.cpu_all_sample)
+    extras["cpu_baselines"]["seconds"] = round(time.perf_counter() - t0, 1)
+    return extras
+
+
 def inlj_workload(args, world, rank, device, stream):
     import numpy as np
     import torch
@@ -432,7 +577,22 @@ def inlj_workload(args, world, rank, device, stream):
     if l2_sectors:
         path_gbs = l2_sectors * 32 * m / (lookup_ms / 1e3) / 1e9
         roofline["index_path"] = {"l2_sectors_per_probe": l2_sectors, "bytes_per_probe": round(l2_sectors * 32, 1),
-                                  "achieved_gbs": round(path_gbs, 1), "frac_of_hbm_peak": round(path_gbs / peak, 4)}
+                                  "l2_to_sm_gbs": round(path_gbs, 1),
+                                  "note": "L2-to-SM bytes of the search pass (ncu sectors x 32 B over the live "
+                                          "kernel time); most index reads are L2 hits"}
+    # the second roofline of scattered probes: each needs at least one random
+    # 32-byte sector of a column larger than L2, so probes/s <= random
+    # sectors/s (measured here, same buffer size class, same 64-byte fill)
+    if 8 * n > L2_BYTES and not args.no_calibration:
+        cal = random_sector_rate(device, stream)
+        peak_sectors = cal["fill_64B"]["sectors_per_s"]
+        probes_per_s = m / (lookup_ms / 1e3)
+        roofline["random_sector"] = {"bound": "random 32-byte sector reads", "sectors_per_probe": 1,
+                                     "achieved": round(probes_per_s / 1e9, 3), "peak": round(peak_sectors / 1e9, 3),
+                                     "unit": "G sectors/s", "frac": round(probes_per_s / peak_sectors, 4),
+                                     "calibration": cal,
+                                     "peak_source": "gj_calibrate_random_sectors in this run (2 GiB buffer, "
+                                                    "64-byte L2 fill, best of 5)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -470,6 +630,13 @@ def inlj_workload(args, world, rank, device, stream):
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.no_extras:
+        headline_ix.free()
+        del pairs, ws, expect
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        line["north_star"] = north_star_extras(args, world, device, stream, keys, h_keys, h_probes)
+        line["north_star"]["seconds"] = round(time.perf_counter() - t0, 1)
     return line
 
 
@@ -485,44 +652,34 @@ def _base_line(args, world, metric, value, unit, ms_per_step, workload, extra):
     return line
 
 
-def partitioned_workload(args, world, rank, device, stream):
-    """Partitioned INLJ at out-of-L2 scale: 2^28-key index, 2^29 Zipf(0.5)
-    probes, range partition with an autotuned fanout (2^8..2^12) and window,
-    pairs emitted in partition order."""
+def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind="btree", sample_clocks=True):
+    """Partitioned INLJ of 2^m_log2 Zipf(theta) probes into a 2^n_log2-key
+    index: fanout and window from the library's autotuner (unless given),
+    timed steps, pairs checked against the oracle on a seeded sample of probe
+    rows, and the unpartitioned pairs on the same probes for comparison."""
     import ctypes
 
+    import numpy as np
     import torch
 
     import gpujoin_gb300 as gj
 
-    n_log2 = args.n_log2 if args.n_log2 != 26 else 28
-    m_log2 = args.m_log2 if args.m_log2 != 28 else 29
     n, m = 1 << n_log2, 1 << m_log2
     keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
     probes = gj.generate_probes(keys, m, theta=args.theta, seed=args.seed + 1)
-    kind = args.indexes.split(",")[0]
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
-
-    # fanout and window (and for a B+tree its node format) from the library's
-    # autotuners, on the same probes, unless given
-    tune = None
     params = index_params(args, kind)
+    ix = gj.make_index(kind, **params).construct(None, keys)
+    tune = None
     if args.radix_bits and args.window:
         bits, window = args.radix_bits, min(args.window, m)
-    elif kind == "btree" and not params:
-        w, lk, bits, window, tuned_ms = gj.autotune_partitioned_btree(keys, probes)
-        params = {"btree_node_keys": w, "btree_leaf_keys": lk}
-        tune = {"btree_node_keys": w, "btree_leaf_keys": lk, "radix_bits": bits, "window": window,
-                "ms": round(tuned_ms, 3)}
     else:
-        ix = gj.make_index(kind, **params).construct(None, keys)
         bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
-        tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3)}
-        ix.free()
-    ix = gj.make_index(kind, **params).construct(None, keys)
+        tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3),
+                "candidates": "fanout 2^8..2^12 x window {m, m/4, m/16}"}
     need = ctypes.c_size_t()
-    gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need))
+    gj._check(gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need)))
     ws = torch.empty(need.value, dtype=torch.uint8, device=device)
 
     def step():
@@ -530,43 +687,59 @@ def partitioned_workload(args, world, rank, device, stream):
                                                 pairs.data_ptr(), count.data_ptr(), ws.data_ptr(), ws.numel(),
                                                 stream.cuda_stream))
 
-    sampler = ClockSampler(device.index)
-    sampler.start()
-    ms = time_steps(step, args.steps, args.warmup, stream, world, device)
-    clocks = sampler.stop()
+    sampler = ClockSampler(device.index) if sample_clocks else None
+    if sampler:
+        sampler.start()
+    ms = time_steps(step, steps, args.warmup, stream, world, device)
+    clocks = sampler.stop() if sampler else None
     ms = max_over_ranks(ms, world, device)
     got = int(count.item())
-
+    parity = None
+    if not args.no_parity:
+        sem = "exact" if kind in EXACT_KINDS else "lower_bound"
+        parity = check_pairs_sample(pairs, count, m, keys.cpu().numpy().view(np.uint64),
+                                    probes.cpu().numpy().view(np.uint64), args.parity_sample, args.seed + 7, sem)
+        parity["semantics"] = sem
     # the same probes through the unpartitioned pairs kernel, for comparison
     pw = ctypes.c_size_t()
     gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(pw))
     pws = torch.empty(pw.value, dtype=torch.uint8, device=device)
-    plain_ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, pws), max(2, args.steps // 2), 1, stream, world,
-                          device) / max(2, args.steps // 2)
-
-    import numpy as np
-
-    sem = "exact" if kind in EXACT_KINDS else "lower_bound"
-    parity = check_pairs_sample(pairs, count, m, keys.cpu().numpy().view(np.uint64),
-                                probes.cpu().numpy().view(np.uint64), args.parity_sample, args.seed + 7, sem)
-    per_step = ms / args.steps
+    plain_steps = max(2, steps // 2)
+    plain_ms = time_steps(lambda: ix.inlj_pairs(probes, pairs, count, pws), plain_steps, 1, stream, world,
+                          device) / plain_steps
+    per_step = ms / steps
     bpp = 8 + 12 + 12 + 8 + 8.0 * n / m
     peak, peak_kind = measured_peak()
     achieved = bpp * m / (per_step / 1e3) / 1e9
-    windows = (m + window - 1) // window
+    out = {"tuples_per_s": world * m * steps / (ms / 1e3), "ms_per_step": per_step, "build_keys": n, "probes": m,
+           "zipf_theta": args.theta, "index": kind, "params": params or "default build", "radix_bits": bits,
+           "window": window, "pairs": got, "autotune": tune, "parity": parity,
+           "plain_pairs_ms_per_step": plain_ms, "plain_pairs_tuples_per_s": m / (plain_ms / 1e3),
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "bytes_per_probe": bpp,
+                        "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
+           "launches_per_step": 3 + ((m + window - 1) // window) * 8, "clocks": clocks}
+    ix.free()
+    del keys, probes, pairs, ws, pws
+    torch.cuda.empty_cache()
+    return out
+
+
+def partitioned_workload(args, world, rank, device, stream):
+    """Partitioned INLJ at out-of-L2 scale: 2^28-key index, 2^29 Zipf(0.5)
+    probes, range partition with an autotuned fanout (2^8..2^12) and window."""
+    n_log2 = args.n_log2 if args.n_log2 != 26 else 28
+    m_log2 = args.m_log2 if args.m_log2 != 28 else 29
+    kind = args.indexes.split(",")[0]
+    r = partitioned_measure(args, world, device, stream, n_log2, m_log2, args.steps, kind)
     return _base_line(
         args, world, "partitioned INLJ probe tuples/s (1 GB300 per rank), % of HBM roofline",
-        world * m * args.steps / (ms / 1e3), "probe tuples/s", per_step,
-        f"partitioned INLJ: {n} uniform uint64 keys (2^{n_log2}), {m} Zipf({args.theta}) probes (2^{m_log2}), "
-        f"{ix.type_name()} {params or 'default build'}, range partition 2^{bits}, window {window}",
-        {"partitioned": {"radix_bits": bits, "window": window, "pairs": got, "autotune": tune,
-                         "plain_pairs_ms_per_step": plain_ms,
-                         "plain_pairs_tuples_per_s": m / (plain_ms / 1e3)},
-         "parity": parity,
-         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                      "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_probe": bpp,
-                      "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
-         "gpu_launches": args.steps * windows * 6, "clocks": clocks, "cpu_baseline": None, "e2e": None})
+        r["tuples_per_s"], "probe tuples/s", r["ms_per_step"],
+        f"partitioned INLJ: {r['build_keys']} uniform uint64 keys (2^{n_log2}), {r['probes']} Zipf({args.theta}) "
+        f"probes (2^{m_log2}), {kind}, range partition 2^{r['radix_bits']}, window {r['window']}",
+        {"partitioned": r, "parity": r["parity"], "roofline": dict(r["roofline"], traffic=None),
+         "gpu_launches": args.steps * r["launches_per_step"], "clocks": r["clocks"], "cpu_baseline": None,
+         "e2e": None})
 
 
 def host_memory_available() -> int:
@@ -774,7 +947,7 @@ def star_workload(args, world, rank, device, stream):
          "gpu_launches": args.steps, "cpu_baseline": None, "e2e": None})
 
 
-def learned_workload(args, world, rank, device, stream, steps=None):
+def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
     """Learned index against binary search and RadixSpline at exact outputs:
     2^27 keys from three distributions, 2^28 uniformly sampled probes with 5%
     absent keys, lower-bound positions.  The learned index runs as its
@@ -789,9 +962,7 @@ def learned_workload(args, world, rank, device, stream, steps=None):
 
     import gpujoin_gb300 as gj
 
-    steps = steps or args.steps
-    n_log2 = args.n_log2 if args.n_log2 != 26 else 27
-    n, m = 1 << n_log2, 1 << args.m_log2
+    n, m = 1 << n_log2, 1 << m_log2
     results = {}
     out = torch.empty(m, dtype=torch.int32, device=device)
     ref = torch.empty(m, dtype=torch.int32, device=device)
@@ -803,7 +974,7 @@ def learned_workload(args, world, rank, device, stream, steps=None):
                ("learned_mlp", "learned", {"learned_root": gj.LEARNED_ROOT_MLP, **leaves}),
                ("learned_segments", "learned", {"learned_root": gj.LEARNED_ROOT_SEGMENTS, **leaves}),
                ("learned_linear", "learned", {"learned_root": gj.LEARNED_ROOT_LINEAR, **leaves}))
-    if args.learned_quick:
+    if quick:
         configs = configs[:5]
     parity_total = {"checked": 0, "mismatches": 0}
     for dist_name, dist in (("uniform", gj.DIST_UNIFORM), ("lognormal", gj.DIST_LOGNORMAL),
@@ -863,13 +1034,21 @@ def learned_workload(args, world, rank, device, stream, steps=None):
                                      for k in ("binary_search", "radix_spline", f"radix_spline_eps_of_{lname}")}
         results[dist_name] = row
         del keys, probes, present, d_rows, d_want
+    torch.cuda.empty_cache()
+    return results, dict(parity_total, oracle="oracle lower bound on sampled + absent rows")
+
+
+def learned_workload(args, world, rank, device, stream):
+    n_log2 = args.n_log2 if args.n_log2 != 26 else 27
+    results, parity = learned_measure(args, world, device, stream, n_log2, args.m_log2, args.steps, args.learned_quick)
     head = results["uniform"]["learned"]
+    n, m = 1 << n_log2, 1 << args.m_log2
     return _base_line(
         args, world, "learned-index probe tuples/s (1 GB300 per rank), exact lower bounds",
         world * head["tuples_per_s"], "probe tuples/s", head["ms_per_step"],
         f"learned vs plain: {n} keys (2^{n_log2}) x 3 distributions, {m} probes (2^{args.m_log2}) with 5% absent",
-        {"learned": results, "parity": dict(parity_total, oracle="oracle lower bound on sampled + absent rows"),
-         "roofline": None, "gpu_launches": steps, "cpu_baseline": None, "e2e": None})
+        {"learned": results, "parity": parity, "roofline": None, "gpu_launches": args.steps, "cpu_baseline": None,
+         "e2e": None})
 
 
 def batch_workload(args, world, rank, device, stream):
@@ -1032,6 +1211,12 @@ def parse_args(argv=None):
     ap.add_argument("--learned-quick", action="store_true",
                     help="learned: only binary search, RadixSpline and the learned builds at both leaf counts")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (timing runs)")
+    ap.add_argument("--no-calibration", action="store_true", help="inlj: skip the random-sector calibration")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="inlj: only the headline (no partitioned / learned / theta / star / CPU sections)")
+    ap.add_argument("--extra-steps", type=int, default=5, help="timed steps of each extra section")
+    ap.add_argument("--cpu-one-sample", type=int, default=1 << 20, help="CPU baselines: probes at 1 thread")
+    ap.add_argument("--cpu-all-sample", type=int, default=1 << 24, help="CPU baselines: probes at all threads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     return ap.parse_args(argv)

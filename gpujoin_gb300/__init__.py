@@ -140,6 +140,8 @@ _SIGNATURES = {
     "gj_inlj_pairs_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
+    "gj_index_key_range": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
+    "gj_partition_shift": (_i32, [_u64, _u64, _u32, ctypes.POINTER(_u32)]),
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
     "gj_partitioned_inlj_workspace_size": (_i32, [_vp, _u64, _u32, ctypes.POINTER(_sz)]),
@@ -167,6 +169,8 @@ _SIGNATURES = {
     "gj_batch_plan_run": (_i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
     "gj_batch_plan_run_graph": (_i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
     "gj_batch_plan_autotune": (_i32, [_vp, _vp, _vp, _vp, ctypes.POINTER(_u32), ctypes.POINTER(ctypes.c_float)]),
+    "gj_calibrate_sink_words": (_i32, [ctypes.POINTER(_u64)]),
+    "gj_calibrate_random_sectors": (_i32, [_vp, _u64, _u64, _u64, _u32, _vp, _vp]),
     "gj_generate_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_generate_sorted_keys": (_i32, [_vp, _u64, _u32, _u64, _u64, _vp, _sz, _vp]),
     "gj_generate_probes": (_i32, [_vp, _u64, _vp, _u64, ctypes.c_double, ctypes.c_double, _u64, _vp]),

@@ -116,10 +116,11 @@ int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint
                                   uint64_t* window_size, float* best_ms) {
     GJ_CHECK_ARG(node_keys && leaf_keys && radix_bits && window_size, "gj_autotune_partitioned_btree: null argument");
     GJ_CHECK_ARG(n > 0 && d_keys && m > 0 && d_probes, "gj_autotune_partitioned_btree: empty input");
-    // node formats for probes that arrive grouped by key range: the plain
-    // lookup's best (compressed nodes) lengthens each level's dependent chain,
-    // which the partitioned kernel, with fewer warps, hides less well
-    const uint32_t formats[][2] = {{4, 4}, {4, 8}, {4, 16}, {kBtreeCompressed, 4}, {kBtreeCompressed16, 4}};
+    // Partitioned probes search the column slice of their partition through
+    // the partition directory, not the tree's inner levels, so the node
+    // format does not change their time: the default format is built and
+    // the fanout and window are tuned for it.
+    const uint32_t formats[][2] = {{kBtreeCompressed16, 4}};
     float best = -1.f;
     for (const auto& f : formats) {
         gj_index_params p;

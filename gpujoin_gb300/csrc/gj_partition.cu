@@ -26,7 +26,7 @@ namespace {
 
 constexpr int kPartBlock = 512;
 constexpr uint32_t kMaxRadixBits = 12;
-constexpr int kHistUnroll = 4;                                    // keys in flight per thread
+constexpr int kHistUnroll = 8;                                    // keys in flight per thread
 // scatter geometry: block size and resident blocks per SM (its register cap)
 #ifndef GJ_SCATTER_BLOCK
 #define GJ_SCATTER_BLOCK 512
@@ -53,10 +53,12 @@ __host__ __device__ __forceinline__ uint32_t hist_copies(uint32_t fanout) {
     return c;
 }
 
-// hist[p * G + b] = number of keys of block b's chunk in partition p
-__global__ void __launch_bounds__(kPartBlock) k_part_hist(const uint64_t* __restrict__ keys, uint64_t m, uint64_t chunk,
-                                                          uint64_t min_key, uint32_t shift, uint32_t fanout,
-                                                          uint64_t* __restrict__ hist) {
+// hist[p * G + b] = number of keys of block b's chunk in partition p (kB
+// threads a block: 512, or 1024 when the scatter runs one block per SM)
+template <int kB>
+__global__ void __launch_bounds__(kB) k_part_hist(const uint64_t* __restrict__ keys, uint64_t m, uint64_t chunk,
+                                                  uint64_t min_key, uint32_t shift, uint32_t fanout,
+                                                  uint64_t* __restrict__ hist) {
     extern __shared__ uint32_t s_hist[];
     const uint32_t copies = hist_copies(fanout);
     for (uint32_t p = threadIdx.x; p < fanout * copies; p += blockDim.x) s_hist[p] = 0;
@@ -64,16 +66,16 @@ __global__ void __launch_bounds__(kPartBlock) k_part_hist(const uint64_t* __rest
     uint32_t* mine = s_hist + ((threadIdx.x >> 5) & (copies - 1)) * fanout;
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
     const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += (uint64_t)kPartBlock * kHistUnroll) {
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += (uint64_t)kB * kHistUnroll) {
         uint64_t k[kHistUnroll];
 #pragma unroll
         for (int u = 0; u < kHistUnroll; ++u) {
-            const uint64_t j = i + (uint64_t)u * kPartBlock;
+            const uint64_t j = i + (uint64_t)u * kB;
             k[u] = j < b1 ? __ldcs(k64 + j) : 0ull;
         }
 #pragma unroll
         for (int u = 0; u < kHistUnroll; ++u)
-            if (i + (uint64_t)u * kPartBlock < b1) atomicAdd(&mine[part_of(k[u], min_key, shift, fanout)], 1u);
+            if (i + (uint64_t)u * kB < b1) atomicAdd(&mine[part_of(k[u], min_key, shift, fanout)], 1u);
     }
     __syncthreads();
     for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) {
@@ -350,7 +352,11 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
             GJ_CUDA_TRY(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem_scatter));
     }
-    k_part_hist<<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
+    if (pl.wide)
+        k_part_hist<1024><<<pl.nblocks, 1024, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
+    else
+        k_part_hist<kPartBlock><<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift,
+                                                                          pl.fanout, hist);
     GJ_CUDA_TRY(cudaGetLastError());
     GJ_TRY(inclusive_scan_sum(hist, cells, scan_ws, scan_workspace_bytes(cells), s));
     if (d_offsets) {

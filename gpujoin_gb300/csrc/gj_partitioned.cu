@@ -21,7 +21,7 @@
 // call (one pass over the column) into the workspace.
 //
 // A probe block takes one chunk of one partition (up to kChunk probes),
-// copies that partition's directory (at most 128 KB) into shared memory and
+// copies that partition's directory (at most 64 KB) into shared memory and
 // searches each probe with one shared-memory read and, usually, one or two
 // independent sector loads from L2 (the partition's column slice is read by
 // every block of that partition at about the same time).  A partition whose
@@ -47,14 +47,14 @@ namespace gj {
 namespace {
 
 constexpr uint32_t kMaxRadixBits = 12;
-constexpr uint32_t kMaxDirBits = 16;       // 2^16 u16 entries = 128 KB of shared memory
+constexpr uint32_t kMaxDirBits = 15;       // 2^15 u16 entries = 64 KB of shared memory: 3 blocks per SM
 constexpr uint32_t kDirPad = 8;            // D + 1 entries rounded up to a multiple of 8 (16 bytes)
 constexpr uint16_t kDirUnset = 0xFFFF;     // not yet written / offset above 65534
 constexpr uint32_t kDirKeyCap = 16;        // entries one key thread writes; the rest by the fill pass
-constexpr int kProbeBlock = 1024;
-constexpr int kProbeItems = 2;             // probes per thread in flight
+constexpr int kProbeBlock = 256;
+constexpr int kProbeItems = 4;             // probes per thread in flight
 constexpr uint32_t kProbeTile = kProbeBlock * kProbeItems;
-constexpr uint32_t kChunk = 1u << 15;      // probes per block (directory copied once per chunk)
+constexpr uint32_t kChunk = 1u << 14;      // probes per block (directory copied once per chunk)
 
 enum probe_semantics : int { kSemNone = 0, kSemLowerBound = 1, kSemExact = 2 };
 
@@ -132,17 +132,31 @@ __device__ __forceinline__ void dir_put(uint16_t* dir, const uint32_t* bound, ui
 // lower bound is i are those in (G(col[i-1]), G(col[i])] (G = global bucket
 // of a key, monotone); after the last key, every bucket up to F * D - 1 has
 // lower bound n.  A thread writes at most kDirKeyCap of them; k_dir_fill
-// completes longer runs (gaps in the column).
-__global__ void k_dir_keys(const uint64_t* __restrict__ col, uint64_t n, pgeom g, const uint32_t* __restrict__ bound,
-                           uint16_t* __restrict__ dir, uint32_t* __restrict__ wide) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > n) return;
+// completes longer runs (gaps in the column).  kDirKeysPer positions per
+// thread, kDirKeysBlock apart (coalesced loads, several in flight).
+constexpr int kDirKeysBlock = 256;
+constexpr int kDirKeysPer = 8;
+__global__ void __launch_bounds__(kDirKeysBlock) k_dir_keys(const uint64_t* __restrict__ col, uint64_t n, pgeom g,
+                                                            const uint32_t* __restrict__ bound,
+                                                            uint16_t* __restrict__ dir, uint32_t* __restrict__ wide) {
+    const uint64_t i0 = (uint64_t)blockIdx.x * (kDirKeysBlock * kDirKeysPer) + threadIdx.x;
     const uint32_t total = g.fanout << g.dbits;
-    const uint32_t lo = i == 0 ? 0u : global_bucket(ld_ro(col + i - 1), g) + 1u;
-    const uint32_t hi = i == n ? total - 1u : global_bucket(ld_ro(col + i), g);
-    if (lo > hi) return;
-    const uint32_t end = hi - lo >= kDirKeyCap ? lo + kDirKeyCap - 1 : hi;
-    for (uint32_t gb = lo; gb <= end; ++gb) dir_put(dir, bound, wide, g, gb, i);
+    uint32_t cur[kDirKeysPer], prev[kDirKeysPer];
+#pragma unroll
+    for (int k = 0; k < kDirKeysPer; ++k) {
+        const uint64_t i = i0 + (uint64_t)k * kDirKeysBlock;
+        cur[k] = i < n ? global_bucket(__ldcs(reinterpret_cast<const unsigned long long*>(col) + i), g) : total - 1u;
+        prev[k] = (i >= 1 && i - 1 < n) ? global_bucket(ld_ro(col + i - 1), g) + 1u : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kDirKeysPer; ++k) {
+        const uint64_t i = i0 + (uint64_t)k * kDirKeysBlock;
+        if (i > n) break;
+        const uint32_t lo = i == 0 ? 0u : prev[k], hi = cur[k];
+        if (lo > hi) continue;
+        const uint32_t end = hi - lo >= kDirKeyCap ? lo + kDirKeyCap - 1 : hi;
+        for (uint32_t gb = lo; gb <= end; ++gb) dir_put(dir, bound, wide, g, gb, i);
+    }
 }
 
 // Entries left unset by k_dir_keys: the lower bound of the bucket's first
@@ -161,9 +175,11 @@ __global__ void k_dir_fill(const uint64_t* __restrict__ col, uint64_t n, pgeom g
 }
 
 // chunk_begin[p] = number of chunks of the partitions before p (F + 1
-// entries; chunk_begin[F] = total), one block of 1024 threads
+// entries; chunk_begin[F] = total) and chunk_part[c] = the partition of
+// chunk c, one block of 1024 threads
 __global__ void __launch_bounds__(1024) k_chunk_map(const uint64_t* __restrict__ offsets, uint32_t fanout,
-                                                    uint32_t* __restrict__ chunk_begin) {
+                                                    uint32_t* __restrict__ chunk_begin,
+                                                    uint32_t* __restrict__ chunk_part) {
     __shared__ uint32_t s_warp[32];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t per = (fanout + 1023) / 1024;
@@ -197,7 +213,9 @@ __global__ void __launch_bounds__(1024) k_chunk_map(const uint64_t* __restrict__
         const uint32_t p = begin + q;
         if (p < fanout) {
             chunk_begin[p] = run;
-            run += (uint32_t)((offsets[p + 1] - offsets[p] + kChunk - 1) / kChunk);
+            const uint32_t nc = (uint32_t)((offsets[p + 1] - offsets[p] + kChunk - 1) / kChunk);
+            for (uint32_t c = 0; c < nc; ++c) chunk_part[run + c] = p;
+            run += nc;
         }
     }
     if (threadIdx.x == 1023) chunk_begin[fanout] = run;
@@ -246,6 +264,7 @@ struct probe_args {
     const uint32_t* prows;       // their probe rows
     const uint64_t* offsets;     // partition starts in the window (F + 1)
     const uint32_t* chunk_begin; // F + 1
+    const uint32_t* chunk_part;  // partition of each chunk
     const uint16_t* dir;         // F x dir_stride(dbits)
     const uint32_t* bound;       // c_p, F + 1
     const uint32_t* wide;        // F
@@ -258,27 +277,15 @@ struct probe_args {
 };
 
 template <int kSem, bool kAligned>
-__global__ void __launch_bounds__(kProbeBlock, 1) k_part_probe(const __grid_constant__ probe_args a) {
+__global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_constant__ probe_args a) {
     extern __shared__ __align__(16) uint16_t s_dir[];
     constexpr int kWarps = kProbeBlock / 32;
-    __shared__ uint32_t s_p;
     __shared__ uint32_t s_cnt[kWarps * kProbeItems];
     __shared__ unsigned long long s_base;
     const uint32_t c = blockIdx.x;
     const uint32_t F = a.g.fanout;
     if (c >= __ldg(a.chunk_begin + F)) return;
-    if (threadIdx.x == 0) {
-        // the last partition whose first chunk is <= c
-        uint32_t lo = 0, hi = F;  // chunk_begin[lo] <= c < chunk_begin[hi]
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(a.chunk_begin + mid) <= c) lo = mid;
-            else hi = mid;
-        }
-        s_p = lo;
-    }
-    __syncthreads();
-    const uint32_t p = s_p;
+    const uint32_t p = __ldg(a.chunk_part + c);
     const uint64_t pbeg = __ldg(reinterpret_cast<const unsigned long long*>(a.offsets) + p) +
                           (uint64_t)(c - __ldg(a.chunk_begin + p)) * kChunk;
     const uint64_t pend0 = __ldg(reinterpret_cast<const unsigned long long*>(a.offsets) + p + 1);
@@ -295,29 +302,67 @@ __global__ void __launch_bounds__(kProbeBlock, 1) k_part_probe(const __grid_cons
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint64_t t0 = pbeg; t0 < pend; t0 += kProbeTile) {
-        uint32_t res[kProbeItems], row[kProbeItems];
-        bool valid[kProbeItems];
+        // The items of a thread go through each phase together, so their
+        // loads are in flight at the same time: probe keys and rows, then
+        // the first sector of each probe's range, then (for the probes whose
+        // lower bound lies further on) the next sector; anything else (a
+        // longer range, a partial last sector, a wide partition, an
+        // unaligned column) takes the sector binary search.
+        uint64_t key[kProbeItems];
+        uint32_t res[kProbeItems], row[kProbeItems], slo[kProbeItems], shi[kProbeItems];
+        bool valid[kProbeItems], todo[kProbeItems];
 #pragma unroll
         for (int k = 0; k < kProbeItems; ++k) {
             const uint64_t i = t0 + (uint64_t)k * kProbeBlock + threadIdx.x;
             valid[k] = i < pend;
+            key[k] = valid[k] ? __ldcs(reinterpret_cast<const unsigned long long*>(a.pkeys) + i) : 0ull;
+            row[k] = valid[k] ? __ldcs(a.prows + i) : 0u;
             res[k] = kInvalid;
-            row[k] = 0;
-            if (valid[k]) {
-                const uint64_t key = __ldcs(reinterpret_cast<const unsigned long long*>(a.pkeys) + i);
-                row[k] = __ldcs(a.prows + i);
-                if constexpr (kSem != kSemNone) {
-                    bool eq = false;
-                    uint64_t lb;
-                    if (wide) {
-                        lb = lower_bound_sectors(a.col, a.n, c_lo, c_hi, key, kAligned, &eq);
-                    } else {
-                        uint32_t pp, b;
-                        part_bucket(key, a.g, &pp, &b);
-                        lb = lb_in_sectors<kAligned>(a.col, a.n, sbase + s_dir[b], sbase + s_dir[b + 1], key, &eq);
-                    }
-                    if (lb < a.n && (kSem == kSemLowerBound || eq)) res[k] = (uint32_t)lb;
+            todo[k] = kSem != kSemNone && valid[k];
+            slo[k] = shi[k] = 0;
+        }
+        if constexpr (kSem != kSemNone) {
+            if (!wide) {
+#pragma unroll
+                for (int k = 0; k < kProbeItems; ++k) {
+                    uint32_t pp, b;
+                    part_bucket(key[k], a.g, &pp, &b);
+                    slo[k] = (uint32_t)sbase + s_dir[b];
+                    shi[k] = (uint32_t)sbase + s_dir[b + 1];
                 }
+                if constexpr (kAligned) {
+#pragma unroll
+                    for (int step = 0; step < 2; ++step) {
+                        uint64_t w[kProbeItems][4];
+                        bool load[kProbeItems];
+#pragma unroll
+                        for (int k = 0; k < kProbeItems; ++k) {
+                            const uint32_t sct = slo[k] + (uint32_t)step;
+                            load[k] = todo[k] && sct <= shi[k] && ((uint64_t)sct << 2) + 4 <= a.n;
+                            if (load[k]) ld_sector(a.col + ((uint64_t)sct << 2), w[k]);
+                        }
+#pragma unroll
+                        for (int k = 0; k < kProbeItems; ++k) {
+                            if (!load[k]) continue;
+                            const uint64_t x = key[k];
+                            const uint32_t below = (w[k][0] < x) + (w[k][1] < x) + (w[k][2] < x) + (w[k][3] < x);
+                            if (below < 4) {
+                                todo[k] = false;
+                                if (kSem == kSemLowerBound || pick4(w[k], below) == x)
+                                    res[k] = (((uint32_t)slo[k] + (uint32_t)step) << 2) + below;
+                            }
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kProbeItems; ++k) {
+                if (!todo[k]) continue;
+                bool eq = false;
+                const uint64_t lo = wide ? c_lo : (uint64_t)slo[k] << 2;
+                const uint64_t hi = wide ? c_hi : ((((uint64_t)shi[k] + 1) << 2) < a.n ? ((uint64_t)shi[k] + 1) << 2 : a.n);
+                const uint64_t lb = lower_bound_sectors(a.col, a.n, lo, hi, key[k], kAligned, &eq);
+                if (lb < a.n && (kSem == kSemLowerBound || eq)) res[k] = (uint32_t)lb;
             }
         }
         if (a.positions) {
@@ -413,12 +458,15 @@ partitioned_layout layout_for(const gj_index* idx, uint64_t window, uint32_t rad
     return L;
 }
 
+// chunks of a window of w probes: at most one partial chunk per partition
+uint64_t max_chunks(uint64_t w, uint32_t fanout) { return (w + kChunk - 1) / kChunk + fanout; }
+
 size_t partitioned_ws_bytes(const partitioned_layout& L, int sm_count) {
     const uint64_t w = L.window;
     return workspace_carver::need({w * sizeof(uint64_t), w * sizeof(uint32_t), (L.fanout + 1) * sizeof(uint64_t),
                                    partition_ws_bytes(w, L.radix_bits, sm_count), L.dir_entries * sizeof(uint16_t),
                                    (L.fanout + 1) * sizeof(uint32_t), L.fanout * sizeof(uint32_t),
-                                   (L.fanout + 1) * sizeof(uint32_t)});
+                                   (L.fanout + 1) * sizeof(uint32_t), max_chunks(w, L.fanout) * sizeof(uint32_t)});
 }
 
 template <class Kernel>
@@ -431,7 +479,7 @@ template <int kSem, bool kAligned>
 int launch_probe(const probe_args& a, uint64_t len, cudaStream_t s) {
     const size_t smem = kSem == kSemNone ? 0 : (size_t)dir_stride(a.g.dbits) * sizeof(uint16_t);
     GJ_TRY(raise_smem(k_part_probe<kSem, kAligned>, smem));
-    const uint64_t grid = (len + kChunk - 1) / kChunk + a.g.fanout;  // chunks <= ceil(len / C) + F
+    const uint64_t grid = max_chunks(len, a.g.fanout);
     k_part_probe<kSem, kAligned><<<(unsigned)grid, kProbeBlock, smem, s>>>(a);
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
@@ -449,6 +497,21 @@ int dispatch_probe(int sem, bool aligned, const probe_args& a, uint64_t len, cud
 using namespace gj;
 
 extern "C" {
+
+int gj_index_key_range(const gj_index* index, uint64_t* min_key, uint64_t* max_key) {
+    GJ_CHECK_ARG(index && min_key && max_key, "gj_index_key_range: null argument");
+    *min_key = index->min_key;
+    *max_key = index->max_key;
+    return GJ_OK;
+}
+
+int gj_partition_shift(uint64_t min_key, uint64_t max_key, uint32_t radix_bits, uint32_t* shift) {
+    GJ_CHECK_ARG(shift, "gj_partition_shift: null argument");
+    GJ_CHECK_ARG(min_key <= max_key, "gj_partition_shift: min_key > max_key");
+    GJ_CHECK_ARG(radix_bits >= 1 && radix_bits <= kMaxRadixBits, "gj_partition_shift: radix_bits not in [1, 12]");
+    *shift = shift_for(min_key, max_key, radix_bits);
+    return GJ_OK;
+}
 
 int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
                                        size_t* bytes) {
@@ -491,7 +554,8 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
     uint32_t* bound = wc.take<uint32_t>(L.fanout + 1);
     uint32_t* wide = wc.take<uint32_t>(L.fanout);
     uint32_t* chunk_begin = wc.take<uint32_t>(L.fanout + 1);
-    if (!pkeys || !prows || !offsets || !pws || !dir || !bound || !wide || !chunk_begin) {
+    uint32_t* chunk_part = wc.take<uint32_t>(max_chunks(w, L.fanout));
+    if (!pkeys || !prows || !offsets || !pws || !dir || !bound || !wide || !chunk_begin || !chunk_part) {
         set_error("gj_partitioned_inlj: workspace of %zu bytes is smaller than the %zu required", workspace_bytes,
                   partitioned_ws_bytes(L, di.sm_count));
         return GJ_ERR_WORKSPACE;
@@ -514,7 +578,9 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
         GJ_CUDA_TRY(cudaMemsetAsync(dir, 0xFF, L.dir_entries * sizeof(uint16_t), s));
         k_dir_bounds<<<(L.fanout + 1 + 255) / 256, 256, 0, s>>>(col, n, g, bound, dir, wide);
         GJ_CUDA_TRY(cudaGetLastError());
-        k_dir_keys<<<(unsigned)((n + 1 + 255) / 256), 256, 0, s>>>(col, n, g, bound, dir, wide);
+        const uint64_t per_block = (uint64_t)kDirKeysBlock * kDirKeysPer;
+        k_dir_keys<<<(unsigned)((n + 1 + per_block - 1) / per_block), kDirKeysBlock, 0, s>>>(col, n, g, bound, dir,
+                                                                                          wide);
         GJ_CUDA_TRY(cudaGetLastError());
         const uint64_t buckets = (uint64_t)L.fanout << L.dbits;
         k_dir_fill<<<(unsigned)((buckets + 255) / 256), 256, 0, s>>>(col, n, g, bound, dir, wide);
@@ -529,6 +595,7 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
     a.prows = prows;
     a.offsets = offsets;
     a.chunk_begin = chunk_begin;
+    a.chunk_part = chunk_part;
     a.dir = dir;
     a.bound = bound;
     a.wide = wide;
@@ -542,7 +609,7 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
         const uint64_t len = std::min<uint64_t>(w, m - off);
         GJ_TRY(range_partition_impl(d_probes + off, len, g.min_key, g.shift, radix_bits, off, pkeys, prows, offsets,
                                     pws, pws_bytes, s));
-        k_chunk_map<<<1, 1024, 0, s>>>(offsets, L.fanout, chunk_begin);
+        k_chunk_map<<<1, 1024, 0, s>>>(offsets, L.fanout, chunk_begin, chunk_part);
         GJ_CUDA_TRY(cudaGetLastError());
         GJ_TRY(dispatch_probe(sem, aligned, a, len, s));
     }

@@ -261,6 +261,13 @@ int gj_inlj_pairs_noalloc(const gj_index* index, const uint64_t* d_probes, uint6
  * one chunk is not fixed.  d_out_keys / d_out_rows hold m entries, d_offsets
  * 2^radix_bits + 1.  radix_bits in [1, 12]. */
 int gj_partition_workspace_size(uint64_t m, uint32_t radix_bits, size_t* bytes);
+/* The key range an index was built over (its column's first and last key),
+ * from which its partitions are cut; no counterpart in the reference, whose
+ * partitioning uses fixed key bits (src/index_lookup_new.cu:63-67). */
+int gj_index_key_range(const gj_index* index, uint64_t* min_key, uint64_t* max_key);
+/* The shift of gj_range_partition that maps [min_key, max_key] onto
+ * 2^radix_bits partitions (the smallest such shift). */
+int gj_partition_shift(uint64_t min_key, uint64_t max_key, uint32_t radix_bits, uint32_t* shift);
 int gj_range_partition(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift,
                        uint32_t radix_bits, uint64_t* d_out_keys, uint32_t* d_out_rows,
                        uint64_t* d_offsets, void* d_workspace, size_t workspace_bytes, void* stream);
@@ -386,12 +393,26 @@ int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uin
                             uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
 int gj_autotune_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m, void* stream,
                       uint32_t* node_keys, uint32_t* leaf_keys, float* best_ms);
-/* B+tree node format (node x leaf width: 4 x 4, 4 x 8, 4 x 16, 7 x 4, 15 x 4) together
- * with partition fanout and window for the partitioned INLJ of these probes:
- * gj_autotune_partitioned on a B+tree of each format. */
+/* B+tree node format together with partition fanout and window for the
+ * partitioned INLJ of these probes.  Partitioned probes search their
+ * partition's column slice through the partition directory, so the node
+ * format does not change their time: the default format (15 x 4) is
+ * returned with gj_autotune_partitioned's fanout and window for it. */
 int gj_autotune_partitioned_btree(const uint64_t* d_keys, uint64_t n, const uint64_t* d_probes, uint64_t m,
                                   void* stream, uint32_t* node_keys, uint32_t* leaf_keys, uint32_t* radix_bits,
                                   uint64_t* window_size, float* best_ms);
+
+/* ---- calibration ---------------------------------------------------------- */
+/* The random 32-byte sector read rate, the roofline of scattered probes
+ * whose column does not fit L2 (each needs at least one random sector); no
+ * counterpart in the reference.  Reads m sectors at pseudo-random indexes
+ * (a hash of the load number and seed) of d_buf (n_sectors 32-byte sectors,
+ * 32-byte aligned); fill64 != 0 asks L2 for 64-byte fills on misses, as the
+ * probe kernels' scattered loads do.  d_sink: gj_calibrate_sink_words
+ * uint64 words (the loaded data folded, so that no load is dropped). */
+int gj_calibrate_sink_words(uint64_t* words);
+int gj_calibrate_random_sectors(const uint64_t* d_buf, uint64_t n_sectors, uint64_t m, uint64_t seed,
+                                uint32_t fill64, uint64_t* d_sink, void* stream);
 
 /* ---- synthetic inputs (src/index_lookup_common.cuh:44-206, src/zipf.hpp) --- */
 /* n strictly increasing keys, iid-uniform in distribution over [0, upper)

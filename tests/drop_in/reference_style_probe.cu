@@ -1,14 +1,17 @@
 // A probe written the way the reference's code is written -- index class
 // templates, construct(h_column, d_column), a kernel taking the index's
-// device_index by value and calling cooperative_lookup(active, key) -- built
-// against include/gpujoin/indexes.cuh and libgpujoin.so.  Used by
-// tests/test_drop_in.py to show that such code compiles and probes
-// correctly without changes to its structure.
+// device_index by value and calling cooperative_lookup(active, key), the
+// partitioned path through partitioned_relation<T> and partitioned_lookup,
+// and the experiment_config / parse_options command line -- built against
+// include/gpujoin/indexes.cuh, include/gpujoin/partitioned_relation.hpp and
+// libgpujoin.so.  Used by tests/test_drop_in.py to show that such code
+// compiles and probes correctly without changes to its structure.
 #include <cstdint>
 #include <exception>
 #include <vector>
 
 #include "gpujoin/indexes.cuh"
+#include "gpujoin/partitioned_relation.hpp"
 
 using index_key_t = uint64_t;
 using value_t = uint64_t;
@@ -62,3 +65,66 @@ extern "C" int drop_in_probe(int kind, const index_key_t* d_col, const index_key
 }
 
 extern "C" const char* drop_in_type_name() { return type_name<btree_index<index_key_t, value_t>>::value(); }
+
+// the tuple type of the reference's partitioned relation (fast-interconnects'
+// Tuple<key, value>); the SoA relation here only takes it as a tag
+template <class K, class V>
+struct Tuple {
+    K key;
+    V value;
+};
+
+struct device_allocator_tag {};
+
+template <class IndexType>
+static int run_partitioned(const index_key_t* d_col, const index_key_t* h_col, uint64_t n, const index_key_t* d_keys,
+                           uint64_t m, uint32_t bits, uint32_t* d_tids) {
+    IndexType index;
+    index.construct(vector_view<index_key_t>(const_cast<index_key_t*>(h_col), n), d_col);
+    device_allocator_tag alloc;
+    partitioned_relation<Tuple<index_key_t, value_t>> rel(m, 1, bits, alloc);
+    partition_offsets offs(1, bits, alloc);
+    range_partition(index, d_keys, m, rel);
+    partitioned_lookup(index, rel, d_tids);
+    return cudaDeviceSynchronize() == cudaSuccess && rel.padding_length() == 0 &&
+                   offs.offsets.size() == gpu_prefix_sum::fanout(bits) + 1
+               ? 0
+               : 2;
+}
+
+extern "C" int drop_in_partitioned_probe(int kind, const index_key_t* d_col, const index_key_t* h_col, uint64_t n,
+                                         const index_key_t* d_keys, uint64_t m, uint32_t bits, uint32_t* d_tids) {
+    try {
+        if (kind == 0) return run_partitioned<btree_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, bits, d_tids);
+        if (kind == 2)
+            return run_partitioned<binary_search_index<index_key_t, value_t>>(d_col, h_col, n, d_keys, m, bits, d_tids);
+        return 3;
+    } catch (const std::exception&) {
+        return 1;
+    }
+}
+
+// parse_options on a reference-style command line; out[] = the parsed
+// fields, return 0, 1 when -h was given, -1 when parsing threw
+extern "C" int drop_in_parse_options(int argc, char** argv, uint64_t* out, char* approach, char* index) {
+    get_experiment_config() = experiment_config();
+    try {
+        const bool help = parse_options(argc, argv);
+        const experiment_config& c = get_experiment_config();
+        out[0] = c.num_elements;
+        out[1] = c.num_lookups;
+        out[2] = c.max_bits;
+        out[3] = c.partitioning_approach_window_size;
+        out[4] = (uint64_t)c.dataset;
+        out[5] = (uint64_t)c.lookup_pattern;
+        out[6] = c.sorted_lookups ? 1 : 0;
+        out[7] = (uint64_t)c.block_size;
+        out[8] = (uint64_t)(c.zipf_factor * 1000.0 + 0.5);
+        out[9] = radix_bits;
+        std::strncpy(approach, c.approach.c_str(), 31);
+        std::strncpy(index, c.index_type.c_str(), 31);
+        return help ? 1 : 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}

@@ -1,7 +1,10 @@
 """Reference-style code (index class templates, device_index by value,
-cooperative_lookup in the kernel) compiled against include/gpujoin/indexes.cuh
-and libgpujoin.so: it compiles here, and on a GPU its results equal the
-oracle's."""
+cooperative_lookup in the kernel, partitioned_relation<T> with
+range_partition / partitioned_lookup, experiment_config and parse_options)
+compiled against include/gpujoin/indexes.cuh,
+include/gpujoin/partitioned_relation.hpp and libgpujoin.so: it compiles
+here, parses the reference's command line, and on a GPU its results equal
+the oracle's."""
 import ctypes
 import os
 import subprocess
@@ -61,3 +64,53 @@ def test_reference_style_code_probes(tmp_path, orc, gj, cuda, kind, name):
         exp = orc.bs_lookup(col, pr)
     exp64 = np.where(exp == 0xFFFFFFFF, np.uint64(0xFFFFFFFFFFFFFFFF), exp.astype(np.uint64))
     np.testing.assert_array_equal(got, exp64)
+
+
+def _parse(lib, args):
+    argv = (ctypes.c_char_p * (len(args) + 1))(b"index_lookup", *[a.encode() for a in args])
+    out = (ctypes.c_uint64 * 10)()
+    approach, index = ctypes.create_string_buffer(32), ctypes.create_string_buffer(32)
+    rc = lib.drop_in_parse_options(len(args) + 1, argv, out, approach, index)
+    return rc, list(out), approach.value.decode(), index.value.decode()
+
+
+def test_reference_command_line_parses(tmp_path, gj):
+    lib = ctypes.CDLL(build_drop_in(tmp_path))
+    lib.drop_in_parse_options.restype = ctypes.c_int
+    # the reference's defaults (src/index_lookup_config.hpp:18-34)
+    rc, out, approach, index = _parse(lib, [])
+    assert rc == 0 and (approach, index) == ("plain", "btree")
+    assert out == [1000000, 100000000, 0, 10000, 1, 0, 0, 128, 1250, 11]
+    # short and long forms as scripts/bench_join.sh writes them
+    rc, out, approach, index = _parse(lib, ["-a", "partitioning", "-i", "harmonia", "-e", "67108864", "-l",
+                                            "268435456", "--maxbits=40", "-w", "1048576", "-d", "dense", "-p",
+                                            "zipf", "-z", "0.5", "-s", "-b", "256"])
+    assert rc == 0 and (approach, index) == ("partitioning", "harmonia")
+    assert out == [67108864, 268435456, 40, 1048576, 0, 2, 1, 256, 500, 11]
+    assert _parse(lib, ["-h"])[0] == 1
+    assert _parse(lib, ["--dataset", "skewed"])[0] == -1
+    assert _parse(lib, ["-q"])[0] == -1
+    assert _parse(lib, ["-w"])[0] == -1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,bits", [(0, 8), (0, 11), (2, 4)])
+def test_reference_style_partitioned_probe(tmp_path, orc, gj, cuda, kind, bits):
+    import torch
+
+    lib = ctypes.CDLL(build_drop_in(tmp_path))
+    lib.drop_in_partitioned_probe.restype = ctypes.c_int
+    lib.drop_in_partitioned_probe.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                              ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p]
+    rng = np.random.default_rng(kind * 100 + bits)
+    col = np.sort(np.unique(rng.integers(0, 1 << 63, 70000, dtype=np.uint64)))[:65536]
+    pr = np.concatenate([col[rng.integers(0, len(col), 30000)], rng.integers(0, 1 << 63, 7000, dtype=np.uint64)])
+    d_col = torch.from_numpy(col.view(np.int64)).cuda()
+    d_pr = torch.from_numpy(pr.view(np.int64)).cuda()
+    out = torch.empty(len(pr), dtype=torch.int32, device="cuda")
+    rc = lib.drop_in_partitioned_probe(kind, d_col.data_ptr(), col.ctypes.data, len(col), d_pr.data_ptr(), len(pr),
+                                       bits, out.data_ptr())
+    assert rc == 0
+    got = out.cpu().numpy().view(np.uint32)
+    exp = orc.exact_lookup(col, pr) if kind == 0 else orc.bs_lookup(col, pr)
+    np.testing.assert_array_equal(got, exp)
