@@ -145,6 +145,7 @@ _SIGNATURES = {
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
     "gj_partitioned_inlj_workspace_size": (_i32, [_vp, _u64, _u32, ctypes.POINTER(_sz)]),
+    "gj_index_prepare_partitioned": (_i32, [_vp, _vp]),
     "gj_partitioned_inlj": (_i32, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_tpch_load_q14": (_i32, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(gj_q14_tables)]),
     "gj_tpch_free_q14": (None, [ctypes.POINTER(gj_q14_tables)]),
@@ -423,6 +424,12 @@ class abstract_index:
         _check(lib().gj_inlj_pairs_noalloc(self.handle, _ptr(d_probes), d_probes.numel(), _ptr(out_pairs),
                                            _ptr(out_count), _stream(stream)))
         return out_pairs, out_count
+
+    def prepare_partitioned(self, stream=None):
+        """Build and keep the partition directory partitioned_inlj probes
+        through (otherwise it is built per call in the workspace)."""
+        _check(lib().gj_index_prepare_partitioned(self.handle, _stream(stream)))
+        return self
 
     def partitioned_inlj(self, d_probes, window_size: int = 0, radix_bits: int = 0, positions: bool = True,
                          pairs: bool = False, workspace=None, stream=None):

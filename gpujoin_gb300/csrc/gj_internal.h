@@ -122,6 +122,11 @@ struct gj_index {
     double learned_init_loss = 0.0;     // root MLP: sample loss of the quantile start
     double learned_trained_loss = 0.0;  // root MLP: sample loss after training
 
+    // partition directory of the partitioned INLJ (gj_index_prepare_partitioned):
+    // sector of the lower bound per key bucket, 2^pdir_bits + 4 entries, or null
+    const uint32_t* pdir = nullptr;
+    uint32_t pdir_bits = 0;
+
     size_t smem_bytes = 0;          // dynamic shared memory of the lookup kernels
     const uint64_t* smem_src = nullptr;  // device source of the staged cache
     uint32_t smem_words = 0;        // 64-bit words staged

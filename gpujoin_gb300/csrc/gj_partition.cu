@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(kScatterBlock, kScatterPerSM) k_part_scatter(c
     uint32_t* s_rows = reinterpret_cast<uint32_t*>(s_dst + fanout);              // kScatterTile
     uint32_t* s_cnt = s_rows + kScatterTile;                                     // fanout
     uint32_t* s_start = s_cnt + fanout;                                          // fanout
+    unsigned long long* s_delta = reinterpret_cast<unsigned long long*>(s_start + fanout);  // fanout
     for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) {
         const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
         s_dst[p] = cell == 0 ? 0ull : incl[cell - 1];
@@ -188,11 +189,12 @@ __global__ void __launch_bounds__(kScatterBlock, kScatterPerSM) k_part_scatter(c
                 s_rows[q] = (uint32_t)(row_base + t0 + j);
             }
         }
+        // output index of the tile's j-th sorted key = s_delta[p] + j
+        for (uint32_t p = threadIdx.x; p < fanout; p += blockDim.x) s_delta[p] = s_dst[p] - s_start[p];
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < tn; j += kScatterBlock) {
             const uint64_t k = s_keys[j];
-            const uint32_t p = part_of(k, min_key, shift, fanout);
-            const uint64_t d = s_dst[p] + (j - s_start[p]);
+            const uint64_t d = s_delta[part_of(k, min_key, shift, fanout)] + j;
             __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
             __stcg(out_rows + d, s_rows[j]);
         }
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(kScatterBlock, kScatterPerSM) k_part_scatter(c
 }
 
 size_t scatter_smem_bytes(uint32_t fanout) {
-    return (size_t)kScatterTile * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)fanout * (8 + 4 + 4);
+    return (size_t)kScatterTile * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)fanout * (8 + 4 + 4 + 8);
 }
 
 // The scatter for fanouts of 2^9 and more: the same counting sort per tile,
@@ -227,7 +229,8 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
     unsigned long long* s_dst = s_mem + kWideTile;                     // fanout: next output slot
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_dst + fanout);     // fanout
     uint32_t* s_start = s_cnt + fanout;                                // fanout
-    uint16_t* s_off = reinterpret_cast<uint16_t*>(s_start + fanout);   // kWideTile
+    unsigned long long* s_delta = reinterpret_cast<unsigned long long*>(s_start + fanout);  // fanout
+    uint16_t* s_off = reinterpret_cast<uint16_t*>(s_delta + fanout);   // kWideTile
     for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) {
         const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
         s_dst[p] = cell == 0 ? 0ull : incl[cell - 1];
@@ -274,11 +277,12 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
                 s_off[q] = (uint16_t)j;
             }
         }
+        // output index of the tile's j-th sorted key = s_delta[p] + j
+        for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) s_delta[p] = s_dst[p] - s_start[p];
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < tn; j += kWideBlock) {
             const uint64_t k = s_keys[j];
-            const uint32_t p = part_of(k, min_key, shift, fanout);
-            const uint64_t d = s_dst[p] + (j - s_start[p]);
+            const uint64_t d = s_delta[part_of(k, min_key, shift, fanout)] + j;
             __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
             __stcg(out_rows + d, (uint32_t)(row_base + t0 + s_off[j]));
         }
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
 }
 
 size_t scatter_wide_smem_bytes(uint32_t fanout) {
-    return (size_t)kWideTile * (sizeof(uint64_t) + sizeof(uint16_t)) + (size_t)fanout * (8 + 4 + 4);
+    return (size_t)kWideTile * (sizeof(uint64_t) + sizeof(uint16_t)) + (size_t)fanout * (8 + 4 + 4 + 8);
 }
 
 struct partition_plan {

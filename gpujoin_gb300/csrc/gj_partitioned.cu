@@ -19,9 +19,11 @@
 // column sector(s): two dependent loads, both L2 hits because the probes of a
 // partition touch one slice of the directory and the column, which stay in
 // L2 while the partition is probed.  The directory depends only on the
-// index; it is built once per call into the workspace: each column position
-// marks the first bucket whose lower bound it is, and a prefix maximum fills
-// the buckets in between (gaps of any length, in linear time).
+// index, so gj_index_prepare_partitioned builds it once and keeps it with
+// the index (like the B+tree's start table); an index that was not prepared
+// gets it built per call into the workspace.  Each column position marks the
+// first bucket whose lower bound it is, and a prefix maximum fills the
+// buckets in between (gaps of any length, in linear time).
 //
 // The search returns the lower bound, from which each index kind's result
 // follows (src/indexes.cuh): the lower bound (binary search, RadixSpline,
@@ -40,6 +42,8 @@
 #include "gj_internal.h"
 
 namespace gj {
+int device_alloc_for(gj_index* idx, size_t bytes, void** out);  // gj_index.cu
+
 namespace {
 
 constexpr uint32_t kMaxRadixBits = 12;
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
     const uint64_t pend = a.len - pbeg < kChunk ? a.len : pbeg + kChunk;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint64_t t0 = pbeg; t0 < pend; t0 += kProbeTile) {
-        uint32_t res[kProbeItems], row[kProbeItems];
+        uint32_t res[kProbeItems];
         bool valid[kProbeItems];
         // keys of the first batch; each batch loads the next one's before it searches
         uint64_t nkey[kProbeBatch];
@@ -254,14 +258,18 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
                 const uint64_t i = t0 + (uint64_t)(r + k) * kProbeBlock + threadIdx.x;
                 key[k] = nkey[k];
                 valid[r + k] = i < pend;
-                row[r + k] = valid[r + k] ? __ldcs(a.prows + i) : 0u;
                 res[r + k] = kInvalid;
                 todo[k] = kSem != kSemNone && valid[r + k];
                 slo[k] = shi[k] = 0;
                 if (kSem != kSemNone && todo[k]) {
+                    // entries b and b + 1: one 16-byte load unless b is the
+                    // last of its four (the directory is padded to whole
+                    // groups of four, so the aligned load stays inside it)
                     const uint32_t b = bucket_of(key[k], a.g);
-                    slo[k] = __ldg(a.dir + b);
-                    shi[k] = __ldg(a.dir + b + 1);
+                    const uint4 e = __ldg(reinterpret_cast<const uint4*>(a.dir) + (b >> 2));
+                    const uint32_t q = b & 3u;
+                    slo[k] = q == 0 ? e.x : q == 1 ? e.y : q == 2 ? e.z : e.w;
+                    shi[k] = q == 0 ? e.y : q == 1 ? e.z : q == 2 ? e.w : __ldg(a.dir + b + 1);
                 }
             }
             if (r + kProbeBatch < kProbeItems) {
@@ -333,6 +341,13 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
                     if (lb < a.n && (kSem == kSemLowerBound || eq)) res[r + k] = (uint32_t)lb;
                 }
             }
+        }
+        // probe rows are read only now, when the results are written
+        uint32_t row[kProbeItems];
+#pragma unroll
+        for (int k = 0; k < kProbeItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kProbeBlock + threadIdx.x;
+            row[k] = valid[k] ? __ldcs(a.prows + i) : 0u;
         }
         if (a.positions) {
 #pragma unroll
@@ -422,16 +437,17 @@ partitioned_layout layout_for(const gj_index* idx, uint64_t window, uint32_t rad
     L.window = window;
     L.radix_bits = radix_bits;
     L.dir_bits = dir_bits_for(idx->n);
-    L.dir_entries = (1ull << L.dir_bits) + 1;
+    L.dir_entries = (1ull << L.dir_bits) + 4;  // the closing entry, then padding to whole 16-byte groups
     L.scan_tiles = (L.dir_entries + kScanTile - 1) / kScanTile;
     return L;
 }
 
-size_t partitioned_ws_bytes(const partitioned_layout& L, int sm_count) {
+size_t partitioned_ws_bytes(const partitioned_layout& L, int sm_count, bool prepared) {
     const uint64_t w = L.window;
     return workspace_carver::need({w * sizeof(uint64_t), w * sizeof(uint32_t),
-                                   partition_ws_bytes(w, L.radix_bits, sm_count), L.dir_entries * sizeof(uint32_t),
-                                   L.scan_tiles * sizeof(uint32_t)});
+                                   partition_ws_bytes(w, L.radix_bits, sm_count),
+                                   prepared ? 0 : L.dir_entries * sizeof(uint32_t),
+                                   prepared ? 0 : L.scan_tiles * sizeof(uint32_t)});
 }
 
 template <int kSem, bool kAligned>
@@ -499,7 +515,24 @@ int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_si
     GJ_CHECK_ARG(radix_bits <= kMaxRadixBits, "gj_partitioned_inlj_workspace_size: radix_bits > 12");
     device_info di;
     GJ_TRY(current_device_info(&di));
-    *bytes = partitioned_ws_bytes(layout_for(index, window_size, radix_bits), di.sm_count);
+    *bytes = partitioned_ws_bytes(layout_for(index, window_size, radix_bits), di.sm_count, index->pdir != nullptr);
+    return GJ_OK;
+}
+
+int gj_index_prepare_partitioned(gj_index* index, void* stream) {
+    GJ_CHECK_ARG(index, "gj_index_prepare_partitioned: null index");
+    if (index->pdir || semantics_of(index) == kSemNone) return GJ_OK;
+    const partitioned_layout L = layout_for(index, 1, 8);
+    void* dir = nullptr;
+    void* tiles = nullptr;
+    GJ_TRY(device_alloc_for(index, L.dir_entries * sizeof(uint32_t), &dir));
+    GJ_TRY(device_alloc_for(index, L.scan_tiles * sizeof(uint32_t), &tiles));
+    cudaStream_t s = as_stream(stream);
+    GJ_TRY(build_directory(index, L, static_cast<uint32_t*>(dir), static_cast<uint32_t*>(tiles), s));
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    index->pdir = static_cast<const uint32_t*>(dir);
+    index->pdir_bits = L.dir_bits;
+    index->bytes += (L.dir_entries + L.scan_tiles) * sizeof(uint32_t);
     return GJ_OK;
 }
 
@@ -527,23 +560,24 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
     uint32_t* prows = wc.take<uint32_t>(w);
     const size_t pws_bytes = partition_ws_bytes(w, radix_bits, di.sm_count);
     void* pws = wc.take<char>(pws_bytes);
-    uint32_t* dir = wc.take<uint32_t>(L.dir_entries);
-    uint32_t* tiles = wc.take<uint32_t>(L.scan_tiles);
-    if (!pkeys || !prows || !pws || !dir || !tiles) {
+    const bool prepared = index->pdir != nullptr;
+    uint32_t* dir = prepared ? nullptr : wc.take<uint32_t>(L.dir_entries);
+    uint32_t* tiles = prepared ? nullptr : wc.take<uint32_t>(L.scan_tiles);
+    if (!pkeys || !prows || !pws || (!prepared && (!dir || !tiles))) {
         set_error("gj_partitioned_inlj: workspace of %zu bytes is smaller than the %zu required", workspace_bytes,
-                  partitioned_ws_bytes(L, di.sm_count));
+                  partitioned_ws_bytes(L, di.sm_count, prepared));
         return GJ_ERR_WORKSPACE;
     }
     if (d_pairs) GJ_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
     if (m == 0) return GJ_OK;
 
     const int sem = semantics_of(index);
-    if (sem != kSemNone) GJ_TRY(build_directory(index, L, dir, tiles, s));
+    if (sem != kSemNone && !prepared) GJ_TRY(build_directory(index, L, dir, tiles, s));
     const uint32_t pshift = shift_for(index->min_key, index->max_key, radix_bits);
     probe_args a;
     a.pkeys = pkeys;
     a.prows = prows;
-    a.dir = dir;
+    a.dir = prepared ? index->pdir : dir;
     a.col = index->d_col;
     a.n = index->n;
     a.g.min_key = index->min_key;

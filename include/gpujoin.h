@@ -289,6 +289,12 @@ int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, co
  * the index size.  Workspace: gj_partitioned_inlj_workspace_size. */
 int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
                                        size_t* bytes);
+/* Builds the index's partition directory (the radix table over its column
+ * that gj_partitioned_inlj probes through, about 2 bytes per key) and keeps
+ * it with the index, like the B+tree's start table; later partitioned calls
+ * skip building it and need less workspace.  Synchronous; idempotent.  No
+ * counterpart in the reference. */
+int gj_index_prepare_partitioned(gj_index* index, void* stream);
 int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint64_t window_size,
                         uint32_t radix_bits, uint32_t* d_positions, uint32_t* d_pairs, uint64_t* d_count,
                         void* d_workspace, size_t workspace_bytes, void* stream);

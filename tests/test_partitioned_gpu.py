@@ -1,10 +1,11 @@
-"""The partitioned INLJ's partition directory on the columns that stress it,
-against the oracle: a partition whose column slice is too wide for 16-bit
-directory offsets (searched over its whole slice), a column that is not
-32-byte aligned, columns of a few keys, clustered keys with long gaps
-(directory entries filled by the fill pass), probes outside the key range,
-and several windows.  Positions must equal the oracle's per probe row, the
-pairs as a set (their order across tiles is not fixed)."""
+"""The partitioned INLJ's directory on the columns that stress it, against
+the oracle: a column whose keys crowd into a few buckets (long lower-bound
+ranges, searched past the first sectors), a column that is not 32-byte
+aligned, columns of a few keys, clustered keys with long gaps (buckets
+filled by the prefix maximum), probes outside the key range, several
+windows, and the directory built per call or kept with the index.
+Positions must equal the oracle's per probe row, the pairs as a set (their
+order across tiles is not fixed)."""
 import numpy as np
 import pytest
 
@@ -31,9 +32,10 @@ def _column(case, rng):
     return column(rng, 100_003)  # "unaligned" and "plain"
 
 
+@pytest.mark.parametrize("prepared", [False, True])
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("case", ["wide", "unaligned", "tiny", "clusters"])
-def test_partitioned_directory_cases(orc, gj, cuda, kind, case):
+def test_partitioned_directory_cases(orc, gj, cuda, kind, case, prepared):
     import torch
 
     rng = np.random.default_rng(len(case) * 31 + len(kind))
@@ -46,6 +48,8 @@ def test_partitioned_directory_cases(orc, gj, cuda, kind, case):
     else:
         d_col = to_dev(torch, col)
     ix = gj.make_index(kind).construct(None, d_col)
+    if prepared:  # the directory kept with the index instead of built per call
+        ix.prepare_partitioned()
     exp = expected(orc, kind, col, pr)
     erows, epos = orc.pairs_from_positions(exp)
     for bits, window in ((8, 0), (12, 0), (10, 7777)):
