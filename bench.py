@@ -252,7 +252,7 @@ def check_pairs_sample(pairs, count, m, h_keys, h_probes, sample, seed, semantic
     by_row = torch.full((m,), -1, dtype=torch.int32, device=pairs.device)
     by_row[p[:, 0].long()] = p[:, 1]
     rng = np.random.default_rng(seed)
-    rows = np.unique(rng.integers(0, m, size=sample))
+    rows = rng.integers(0, m, size=min(sample, m))  # with replacement: a row drawn twice is checked twice
     lb, ex = oracle.fast_positions(h_keys, h_probes[rows], oracle.hardware_threads())
     want = (ex if semantics == "exact" else lb).view(np.int32)
     have = by_row[torch.from_numpy(rows).to(pairs.device)].cpu().numpy()
@@ -995,7 +995,7 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
         present = (ref != -1) & (keys[ref.clamp(min=0).long()] == probes)
         absent_rows = torch.nonzero(~present).squeeze(1).cpu().numpy()
         rng = np.random.default_rng(args.seed + 20 + dist)
-        rows = np.union1d(rng.integers(0, m, size=min(args.parity_sample, m)), absent_rows)
+        rows = np.concatenate([rng.integers(0, m, size=min(args.parity_sample, m)), absent_rows])
         h_keys = keys.cpu().numpy().view(np.uint64)
         h_sel = probes[torch.from_numpy(rows).to(device)].cpu().numpy().view(np.uint64)
         want_lb, _ = oracle_positions(h_keys, h_sel)
@@ -1149,8 +1149,15 @@ def reference_main(args):
         return
     n, m = 1 << args.n_log2, 1 << args.m_log2
     rng = np.random.default_rng(args.seed)
-    keys = np.unique(rng.integers(0, 1 << 63, size=n + n // 64, dtype=np.uint64))
-    keys = np.sort(rng.choice(keys, size=n, replace=False)) if len(keys) > n else keys
+    # n unique sorted uniform keys: draw a few extra, sort, drop repeats, then
+    # drop a seeded random subset of the surplus (keeps the order sorted)
+    keys = np.sort(rng.integers(0, 1 << 63, size=n + n // 64, dtype=np.uint64))
+    keys = keys[np.concatenate([[True], keys[1:] != keys[:-1]])]
+    if len(keys) > n:
+        drop = rng.choice(len(keys), size=len(keys) - n, replace=False)
+        keep = np.ones(len(keys), dtype=bool)
+        keep[drop] = False
+        keys = keys[keep]
     threads = oracle.hardware_threads()
     sample = min(args.ref_sample, m)
     probes = oracle.zipf_probes(keys, sample, args.theta, args.seed + 1, threads)

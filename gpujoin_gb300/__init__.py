@@ -130,6 +130,7 @@ _SIGNATURES = {
     "gj_index_size": (_u64, [_vp]),
     "gj_index_learned_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)]),
     "gj_index_learned_root": (_i32, [_vp, ctypes.POINTER(_u32)]),
+    "gj_index_learned_losses": (_i32, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gj_index_device_view": (_i32, [_vp, _vp, _sz]),
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
@@ -514,6 +515,12 @@ class learned_index(abstract_index):
         r = _u32(0)
         _check(lib().gj_index_learned_root(self.handle, ctypes.byref(r)))
         return r.value
+
+    def losses(self) -> Tuple[float, float]:
+        """MLP root: sample loss at the quantile start and after training."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().gj_index_learned_losses(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return float(a.value), float(b.value)
 
     def stats(self) -> Tuple[int, float]:
         me = _u64(0)

@@ -801,6 +801,17 @@ int gj_index_learned_root(const gj_index* index, uint32_t* root) {
     return GJ_OK;
 }
 
+int gj_index_learned_losses(const gj_index* index, double* init_loss, double* trained_loss) {
+    GJ_CHECK_ARG(index && init_loss && trained_loss, "gj_index_learned_losses: null argument");
+    if (index->type != GJ_INDEX_LEARNED || index->params.learned_root != GJ_LEARNED_ROOT_MLP) {
+        set_error("gj_index_learned_losses: not a learned index with an MLP root");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    *init_loss = index->learned_init_loss;
+    *trained_loss = index->learned_trained_loss;
+    return GJ_OK;
+}
+
 int gj_index_device_view(const gj_index* index, void* view, size_t view_bytes) {
     GJ_CHECK_ARG(index, "gj_index_device_view: null index");
     auto copy = [&](const void* src, size_t bytes) -> int {

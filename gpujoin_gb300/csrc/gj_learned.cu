@@ -533,7 +533,7 @@ int build_learned(gj_index* idx, cudaStream_t s) {
         GJ_CUDA_TRY(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const float b1 = 0.9f, b2 = 0.999f;
         float c1 = 1.f, c2 = 1.f;
-        const uint32_t T = std::max<uint32_t>(1, p.learned_steps);
+        const uint32_t T = p.learned_steps;  // 0: the quantile start, untrained
         for (uint32_t t = 0; t < T; ++t) {
             c1 *= b1;
             c2 *= b2;

@@ -214,7 +214,12 @@ size_t scatter_smem_bytes(uint32_t fanout) {
 // 1024-thread block per SM, and the next tile's keys loaded into registers
 // while the current tile is sorted and written.  A key's place in the tile
 // is kept as a 16-bit offset (its row is row_base + tile start + offset).
-constexpr uint32_t kWideRadixBits = 9;
+// fanout from which the wide scatter runs; GJ_WIDE_RADIX_BITS overrides it
+// in tuning builds
+#ifndef GJ_WIDE_RADIX_BITS
+#define GJ_WIDE_RADIX_BITS 9
+#endif
+constexpr uint32_t kWideRadixBits = GJ_WIDE_RADIX_BITS;
 constexpr int kWideBlock = 1024;
 constexpr int kWideItems = 8;
 constexpr uint32_t kWideTile = kWideBlock * kWideItems;

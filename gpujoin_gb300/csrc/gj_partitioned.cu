@@ -53,6 +53,12 @@ constexpr int kDirPer = 8;                 // column positions (and directory en
 constexpr int kScanBlock = 1024;
 constexpr int kScanPer = 4;
 constexpr uint32_t kScanTile = kScanBlock * kScanPer;
+// load the second sector of a bucket's range together with the first (1),
+// or only when the first holds no key >= the probe (0); GJ_PROBE_SPECULATE
+// overrides it in tuning builds
+#ifndef GJ_PROBE_SPECULATE
+#define GJ_PROBE_SPECULATE 1
+#endif
 constexpr int kProbeBlock = 256;
 constexpr int kProbeBatch = 2;             // probes per thread searched together (loads in flight)
 constexpr int kProbeItems = 8;             // probes per thread and tile (one atomicAdd per tile)
@@ -286,7 +292,7 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
 #pragma unroll
                     for (int k = 0; k < kProbeBatch; ++k) {
                         l0[k] = todo[k] && ((uint64_t)slo[k] << 2) + 4 <= a.n;
-                        l1[k] = l0[k] && shi[k] > slo[k] && ((uint64_t)slo[k] << 2) + 8 <= a.n;
+                        l1[k] = GJ_PROBE_SPECULATE && l0[k] && shi[k] > slo[k] && ((uint64_t)slo[k] << 2) + 8 <= a.n;
                         if (l0[k]) ld_sector(a.col + ((uint64_t)slo[k] << 2), w0[k]);
                         if (l1[k]) ld_sector(a.col + ((uint64_t)slo[k] << 2) + 4, w1[k]);
                     }
@@ -300,6 +306,7 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
                                 if (kSem == kSemLowerBound || pick4(w0[k], b0) == x) res[r + k] = (slo[k] << 2) + b0;
                                 continue;
                             }
+                            if (!l1[k]) slo[k] += 1;  // first sector below the key, second not loaded yet
                         }
                         if (l1[k]) {
                             const uint32_t b1 = (w1[k][0] < x) + (w1[k][1] < x) + (w1[k][2] < x) + (w1[k][3] < x);
@@ -312,10 +319,11 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
                             slo[k] += 2;  // both sectors below the key: go on from the third
                         }
                     }
-                    // the third sector, for the probes that got this far
+                    // the next sector (the third, or the second when it was
+                    // not loaded with the first), for the probes that got this far
 #pragma unroll
                     for (int k = 0; k < kProbeBatch; ++k) {
-                        l0[k] = todo[k] && l1[k] && slo[k] <= shi[k] && ((uint64_t)slo[k] << 2) + 4 <= a.n;
+                        l0[k] = todo[k] && l0[k] && slo[k] <= shi[k] && ((uint64_t)slo[k] << 2) + 4 <= a.n;
                         if (l0[k]) ld_sector(a.col + ((uint64_t)slo[k] << 2), w0[k]);
                     }
 #pragma unroll

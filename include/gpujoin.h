@@ -92,7 +92,7 @@ typedef struct gj_index_params {
                                    power of two in [2^10, 2^20]) */
     uint32_t learned_root;      /* GJ_LEARNED_ROOT_LINEAR, _MLP, _SEGMENTS or _AUTO (default AUTO) */
     uint32_t learned_hidden;    /* MLP hidden width (default 32, max 32) */
-    uint32_t learned_steps;     /* root training steps (default 600) */
+    uint32_t learned_steps;     /* root training steps (default 600; 0 keeps the MLP's quantile start) */
     uint32_t learned_batch;     /* root training batch (default 8192) */
     float learned_lr;           /* root learning rate (Adam, default 1e-3) */
     uint32_t index_memory;      /* where the index's own arrays live: GJ_INDEX_MEMORY_DEVICE (HBM, default)
@@ -142,6 +142,12 @@ int gj_index_learned_stats(const gj_index* index, uint64_t* max_error, double* m
 /* the root model a learned index was built with (GJ_LEARNED_ROOT_LINEAR,
  * _MLP or _SEGMENTS; the one kept when the build asked for GJ_LEARNED_ROOT_AUTO) */
 int gj_index_learned_root(const gj_index* index, uint32_t* root);
+/* learned index with an MLP root: the mean squared error of the root on its
+ * training sample (positions scaled to [0, 1]) at the quantile start and
+ * after training; the build keeps the network with the smaller one
+ * (learned_steps = 0 keeps the start untrained).  No counterpart in the
+ * reference. */
+int gj_index_learned_losses(const gj_index* index, double* init_loss, double* trained_loss);
 
 /* The index's device view -- the struct passed by value to kernels, like
  * the reference's device_index_t member (src/indexes.cuh:18-22,116-124) --

@@ -145,3 +145,37 @@ def test_learned_auto_root(orc, gj, cuda):
         got = from_dev_u32(ix.lookup(probes))
         np.testing.assert_array_equal(got, orc.bs_lookup(h_keys, probes.cpu().numpy().view(np.uint64)))
     assert picks == {"uniform": "linear", "lognormal": "cdf"}, picks
+
+
+def test_what_training_adds_over_the_quantile_start(orc, gj, cuda):
+    # The MLP root starts as the piecewise-linear CDF through 33 sample
+    # quantiles; Adam then trains it on (key, position) samples and the build
+    # keeps whichever of the two fits the samples better.  learned_steps = 0
+    # keeps the start, so the gain of training is measured directly, at the
+    # learned configuration's 2^14 leaves:
+    #   uniform keys: none -- the start fits better and is kept;
+    #   lognormal, clusters: the sample loss drops, and on the clustered
+    #   column (long trained) the mean search window narrows too.
+    n, leaves = 1 << 22, 1 << 14
+    kw = dict(learned_root=gj.LEARNED_ROOT_MLP, learned_leaves=leaves)
+    for dist in (gj.DIST_UNIFORM, gj.DIST_LOGNORMAL, gj.DIST_CLUSTERS):
+        keys = gj.generate_sorted_keys(n, dist, 1 << 63, seed=130 + dist)
+        start = gj.learned_index(learned_steps=0, **kw).construct(None, keys)
+        trained = gj.learned_index(learned_steps=3000, **kw).construct(None, keys)
+        l_start, l_start2 = start.losses()
+        assert l_start == l_start2, "zero steps keeps the quantile start"
+        l_init, l_trained = trained.losses()
+        assert abs(l_init - l_start) <= 1e-12 * max(1.0, l_start), "the same start"
+        _, w_start = start.stats()
+        _, w_trained = trained.stats()
+        if dist == gj.DIST_UNIFORM:
+            assert l_trained >= l_init and w_trained == w_start, (l_init, l_trained, w_start, w_trained)
+        else:
+            assert l_trained < 0.8 * l_init, (dist, l_init, l_trained)
+        if dist == gj.DIST_CLUSTERS:
+            assert w_trained < 0.9 * w_start, (w_start, w_trained)
+        # lookups exact either way
+        probes = gj.generate_probes(keys, 1 << 16, theta=0.0, absent_fraction=0.05, seed=131)
+        want = orc.bs_lookup(keys.cpu().numpy().view(np.uint64), probes.cpu().numpy().view(np.uint64))
+        for ix in (start, trained):
+            np.testing.assert_array_equal(from_dev_u32(ix.lookup(probes)), want)
