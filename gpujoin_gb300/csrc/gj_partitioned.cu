@@ -54,10 +54,12 @@ constexpr int kScanBlock = 1024;
 constexpr int kScanPer = 4;
 constexpr uint32_t kScanTile = kScanBlock * kScanPer;
 // load the second sector of a bucket's range together with the first (1),
-// or only when the first holds no key >= the probe (0); GJ_PROBE_SPECULATE
-// overrides it in tuning builds
+// or only when the first holds no key >= the probe (0, measured faster:
+// 12.11 against 12.45 ms per 2^29 probes -- the kernel is partly bound by
+// the L1 data pipe, which the speculative sector loads fill);
+// GJ_PROBE_SPECULATE overrides it in tuning builds
 #ifndef GJ_PROBE_SPECULATE
-#define GJ_PROBE_SPECULATE 1
+#define GJ_PROBE_SPECULATE 0
 #endif
 constexpr int kProbeBlock = 256;
 constexpr int kProbeBatch = 2;             // probes per thread searched together (loads in flight)
@@ -251,11 +253,11 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
         for (int r = 0; r < kProbeItems; r += kProbeBatch) {
             // kProbeBatch probes of the thread go through each phase
             // together, so that their loads are in flight at the same time:
-            // directory entries; the sector of the first entry and, when the
-            // range goes on, the next one (the lower bound lies in one of the
-            // two for 99.6 % of uniform keys); then the third; anything else
-            // (a longer range, a partial last sector, an unaligned column)
-            // takes the sector binary search.
+            // directory entries; the sector of the first entry (the lower
+            // bound lies there for 75 % of uniform keys at two buckets per
+            // sector); the next sector when the range goes on (99.6 % by
+            // then); anything else (a longer range, a partial last sector, an
+            // unaligned column) takes the sector binary search.
             uint64_t key[kProbeBatch];
             uint32_t slo[kProbeBatch], shi[kProbeBatch];
             bool todo[kProbeBatch];
