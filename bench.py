@@ -3,18 +3,31 @@
 
 Default workload (the headline): an index-nested-loop join of 2^28 probe keys
 drawn Zipf(theta=0.5) with permuted ranks from a 2^26-key uniform build
-column (keys in [0, 2^63)), through a 64-key-node B+tree, emitting
-(probe row, build position) pairs.  Harmonia, RadixSpline, binary search
-and the learned index are measured on the same probes and reported per index.
+column (keys in [0, 2^63)), through the library's default B+tree (inner
+nodes of one 32-byte sector, 15 delta-coded separators; leaves of one
+sector of the column), emitting (probe row, build position) pairs.  The
+B+tree with 64-key uint64 inner nodes (btree_w64, the reference's node
+width), Harmonia, RadixSpline, binary search, the learned index and the hash
+index are measured on the same probes and reported per index; for the
+B+tree, binary search and Harmonia the reference's own device lookups
+(compiled from its headers into oracle/_ref/refgpu.cubin, launched as its
+lookup_kernel) are timed beside this library's lookup on the same data.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--workload inlj|partitioned|star|learned|batch]
 
 A step is one pass of the probe path over the whole probe column.  Inputs
-(2 GiB of probes) are larger than the 126 MB L2, so no flush is needed
+(2 GiB of probes) are larger than the L2, so no flush is needed
 between steps.  For N > 1 (torchrun) every rank runs the same workload on its
 own GPU (independent replicas, no collective on the data path) and the
 timing is the max over ranks.
+
+The default line also carries "north_star", the other configurations of the
+measurement, each checked against the oracle: the B+tree at Zipf theta 0 and
+1.0, the partitioned INLJ (2^29 probes into 2^28 keys), the learned index
+beside binary search and RadixSpline (2^27 keys, three distributions), the
+star-join aggregate and the CPU lookup at 1 and all host threads
+(--no-extras leaves them out).
 
 --impl reference times the reference's CPU lookup path (the B+tree
 restated in oracle/, the reference's page geometry) on the host cores with
@@ -184,6 +197,41 @@ def time_steps(fn, steps: int, warmup: int, stream, world: int, device):
     barrier(world, device)
     torch.cuda.synchronize()
     return start.elapsed_time(end)
+
+
+def reference_gpu_lookup(ref, kind, ix, keys, h_keys, probes, out, expect, steps, warmup, stream, world, device):
+    """Times the reference's own device lookup of `kind` (oracle/ref_gpu.py:
+    its binary_search_index / harmonia_tree lookups compiled from its headers)
+    and this library's lookup (gj_index_lookup, the same u32 positions) on the
+    same index data and probes; both outputs are compared with the oracle's
+    positions."""
+    import torch
+
+    import gpujoin_gb300 as gj
+    from oracle import ref_gpu
+
+    m = probes.numel()
+    if kind == "harmonia":
+        view, keep = ref.padded_harmonia(ref_gpu.harmonia_view(gj, ix))
+        run_ref = lambda: ref.harmonia(view, probes, out, stream)  # noqa: E731
+    elif kind == "btree":
+        # the reference's own tree (246-separator 4 KB pages, 247-key leaves)
+        # over the same column
+        root, keep = ref.btree_pages(keys, h_keys)
+        run_ref = lambda: ref.btree(root, keys, probes, out, stream)  # noqa: E731
+    else:
+        run_ref = lambda: ref.binary_search(keys, probes, out, stream)  # noqa: E731
+    res = {}
+    for arm, fn in (("reference_kernel", run_ref), ("gb300_lookup", lambda: ix.lookup(probes, out=out))):
+        out.fill_(0)
+        ms = max_over_ranks(time_steps(fn, steps, warmup, stream, world, device), world, device)
+        mism = None
+        if expect is not None:
+            mism = int((out != expect).sum().item())
+        res[arm] = {"tuples_per_s": world * m * steps / (ms / 1e3), "ms_per_step": ms / steps, "mismatches": mism}
+    res["speedup"] = round(res["gb300_lookup"]["tuples_per_s"] / res["reference_kernel"]["tuples_per_s"], 2)
+    torch.cuda.synchronize()
+    return res
 
 
 def cpu_baseline_btree(h_keys, h_probes, sample: int):
@@ -477,6 +525,7 @@ def inlj_workload(args, world, rank, device, stream):
     gj.lib().gj_inlj_pairs_workspace_size(m, __import__("ctypes").byref(ws_size))
     ws = torch.empty(ws_size.value, dtype=torch.uint8, device=device)
     headline_index = None
+    ref_kernels = None
     bytes_per_probe = 8 + 8 + (32 if 8 * n > L2_BYTES else 0)
     clocks = None
     for entry in kinds:
@@ -512,6 +561,19 @@ def inlj_workload(args, world, rank, device, stream):
                             "pairs": got, "build_s": round(t_build, 3), "index_bytes": ix.memory_consumption(),
                             "params": params or "default build",
                             "parity": dict(parity, semantics=sem, oracle="all probes") if parity else None}
+        if (entry in ("btree", "harmonia", "binary_search") and rank == 0 and world == 1
+                and not args.no_reference_gpu):
+            # the reference's own device lookup on the same index data
+            try:
+                if ref_kernels is None:
+                    from oracle import ref_gpu
+
+                    ref_kernels = ref_gpu.ReferenceKernels()
+                per_index[entry]["reference_gpu"] = reference_gpu_lookup(
+                    ref_kernels, kind, ix, keys, h_keys, probes, pairs[m:], None if expect is None else expect[sem],
+                    max(3, min(args.steps, args.extra_steps)), args.warmup, stream, world, device)
+            except (OSError, RuntimeError) as e:
+                per_index[entry]["reference_gpu"] = {"unavailable": str(e)}
         if headline_index is None:
             headline_index, headline_ms, headline_ix = kind, ms, ix
         else:
@@ -1225,6 +1287,8 @@ def parse_args(argv=None):
                     help="learned: only binary search, RadixSpline and the learned builds at both leaf counts")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (timing runs)")
     ap.add_argument("--no-calibration", action="store_true", help="inlj: skip the random-sector calibration")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="inlj: skip timing the reference's own device lookups (oracle/_ref/refgpu.cubin)")
     ap.add_argument("--no-extras", action="store_true",
                     help="inlj: only the headline (no partitioned / learned / theta / star / CPU sections)")
     ap.add_argument("--extra-steps", type=int, default=5, help="timed steps of each extra section")

@@ -73,6 +73,11 @@ def lib() -> ctypes.CDLL:
         L.orc_btree_depth.restype = ctypes.c_uint32
         L.orc_btree_depth.argtypes = [_vp]
         L.orc_btree_free.argtypes = [_vp]
+        L.orc_btree_nodes.restype = ctypes.c_uint64
+        L.orc_btree_nodes.argtypes = [_vp]
+        L.orc_btree_write_pages.restype = ctypes.c_int64
+        L.orc_btree_write_pages.argtypes = [_vp, _u8p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                            ctypes.c_uint64, ctypes.c_uint64]
         L.orc_harmonia_build.restype = _vp
         L.orc_harmonia_build.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int)]
         L.orc_harmonia_lookup.restype = None
@@ -139,6 +144,10 @@ def ref_lib() -> Optional[ctypes.CDLL]:
         R.ref_btree_lookup.restype = ctypes.c_int
         R.ref_btree_lookup.argtypes = [_u64p, ctypes.c_uint64, _u64p, ctypes.c_uint64, _u32p,
                                        ctypes.POINTER(ctypes.c_uint32)]
+        R.ref_btree_layout.restype = None
+        R.ref_btree_layout.argtypes = [_u64p]
+        R.ref_btree_canonical.restype = ctypes.c_uint64
+        R.ref_btree_canonical.argtypes = [_u64p, ctypes.c_uint64, _u64p, ctypes.c_uint64]
         R.ref_harmonia_lookup_u64.restype = ctypes.c_int
         R.ref_harmonia_lookup_u64.argtypes = [_u64p, ctypes.c_uint64, _u64p, ctypes.c_uint64, _u32p]
         R.ref_harmonia_arrays_u64.restype = ctypes.c_int
@@ -198,6 +207,19 @@ class BTree:
         out = np.empty(len(probes), dtype=np.uint32)
         lib().orc_btree_lower_bound(self._h, _ptr(probes, _u64p), len(probes), _ptr(out, _u32p), threads)
         return out
+
+    def pages(self, page_bytes: int, keys_off: int, children_off: int, pages_base: int, col_base: int):
+        """The tree in the reference's device page layout (orc_btree_write_pages):
+        (uint8 page image, root node number).  Pointers are formed from
+        pages_base (where the image will be copied) and col_base (the device
+        column)."""
+        nodes = lib().orc_btree_nodes(self._h)
+        out = np.empty(nodes * page_bytes, dtype=np.uint8)
+        root = lib().orc_btree_write_pages(self._h, _ptr(out, _u8p), page_bytes, keys_off, children_off,
+                                           pages_base, col_base)
+        if root < 0:
+            raise ValueError("btree pages: offsets do not fit the page")
+        return out, int(root)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -394,6 +416,52 @@ def ref_btree_lookup(col, probes):
     if rc != 0:
         raise RuntimeError("reference btree build failed")
     return out
+
+
+def ref_btree_layout():
+    """(page size, header size, separator offset, child pointer offset,
+    separators per inner node, keys per leaf) of the reference's uint64
+    B+tree pages, or None without the reference-built checker."""
+    R = ref_lib()
+    if R is None:
+        return None
+    out = np.zeros(6, dtype=np.uint64)
+    R.ref_btree_layout(_ptr(out, _u64p))
+    return [int(v) for v in out]
+
+
+def ref_btree_canonical(col):
+    """The reference's host-built B+tree as ref_btree_canonical's word stream."""
+    R = ref_lib()
+    if R is None:
+        return None
+    col = _u64(col)
+    need = R.ref_btree_canonical(_ptr(col, _u64p), len(col), None, 0)
+    out = np.empty(max(need, 1), dtype=np.uint64)
+    R.ref_btree_canonical(_ptr(col, _u64p), len(col), _ptr(out, _u64p), need)
+    return out[:need]
+
+
+def btree_canonical_from_pages(pages, page_bytes, keys_off, children_off, root, pages_base, col_base):
+    """The same word stream read back from a page image (BTree.pages)."""
+    words = []
+    level = [root]
+    while level:
+        nxt = []
+        for node in level:
+            pg = pages[node * page_bytes:(node + 1) * page_bytes]
+            count = int(pg[:2].view(np.uint16)[0])
+            final = int(pg[3])
+            words += [count, final]
+            words += [int(k) for k in pg[keys_off:keys_off + 8 * count].view(np.uint64)]
+            ptrs = pg[children_off:children_off + 8 * (count + 1)].view(np.uint64)
+            for p in ptrs:
+                if final:
+                    words.append((int(p) - col_base) // 8)
+                else:
+                    nxt.append((int(p) - pages_base) // page_bytes)
+        level = nxt
+    return np.array(words, dtype=np.uint64)
 
 
 def ref_harmonia_lookup(col, probes):

@@ -246,6 +246,31 @@ orc_btree* orc_btree_build(const uint64_t* col, uint64_t n, uint32_t leaf_keys, 
 
 uint32_t orc_btree_depth(const orc_btree* t) { return t->depth; }
 
+uint64_t orc_btree_nodes(const orc_btree* t) { return t->nnodes; }
+
+int64_t orc_btree_write_pages(const orc_btree* t, uint8_t* out, uint64_t page_bytes, uint64_t keys_off,
+                              uint64_t children_off, uint64_t pages_base, uint64_t col_base) {
+    if (keys_off < 4 || keys_off + 8ull * t->inner_keys > children_off ||
+        children_off + 8ull * (t->inner_keys + 1) > page_bytes || (keys_off | children_off) % 8 != 0)
+        return -1;
+    memset(out, 0, t->nnodes * page_bytes);
+    for (uint64_t i = 0; i < t->nnodes; ++i) {
+        const orc_bnode* nd = &t->nodes[i];
+        uint8_t* pg = out + i * page_bytes;
+        const uint16_t count = (uint16_t)nd->count;
+        memcpy(pg, &count, 2);
+        pg[2] = 0;  /* isLeaf: the clustered tree has no leaf pages */
+        pg[3] = (uint8_t)(nd->is_final_inner ? 1 : 0);
+        memcpy(pg + keys_off, nd->keys, 8ull * t->inner_keys);
+        for (uint32_t c = 0; c <= nd->count; ++c) {
+            const uint64_t ptr = nd->is_final_inner ? col_base + 8ull * nd->children[c]
+                                                    : pages_base + page_bytes * nd->children[c];
+            memcpy(pg + children_off + 8ull * c, &ptr, 8);
+        }
+    }
+    return (int64_t)t->root;
+}
+
 /* lookup(): src/btree.cuh:504-531 */
 static uint32_t bt_lookup_one(const orc_btree* t, uint64_t key) {
     uint64_t ref = t->root;

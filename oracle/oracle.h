@@ -54,6 +54,17 @@ void orc_btree_lookup(const orc_btree* t, const uint64_t* probes, uint64_t m,
 void orc_btree_lower_bound(const orc_btree* t, const uint64_t* probes, uint64_t m, uint32_t* out, int threads);
 uint32_t orc_btree_depth(const orc_btree* t);
 void orc_btree_free(orc_btree* t);
+/* The tree as the reference lays it out in device memory (src/btree.cuh:30-64,
+ * migrate :440-476): one page_bytes page per inner node, at page
+ * pages_base + page_bytes * node; header {u16 count, bool isLeaf = 0, bool
+ * isFinalInner} at offset 0; count separators at keys_off (UINT64_MAX after
+ * them); count + 1 child pointers at children_off -- pages of the inner
+ * nodes below, or for a final inner node pointers into the column at
+ * col_base.  out holds orc_btree_nodes() * page_bytes bytes; returns the
+ * root's node number, or -1 if the offsets do not fit the page. */
+uint64_t orc_btree_nodes(const orc_btree* t);
+int64_t orc_btree_write_pages(const orc_btree* t, uint8_t* out, uint64_t page_bytes, uint64_t keys_off,
+                              uint64_t children_off, uint64_t pages_base, uint64_t col_base);
 
 /* Harmonia (src/harmonia.cuh:133-404 construction, :640-668 host lookup),
  * Reuse_Input_Memory: the leaf level is the column itself; n % max_keys == 0. */

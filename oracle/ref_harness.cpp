@@ -98,6 +98,56 @@ int ref_btree_lookup(const uint64_t* col, uint64_t n, const uint64_t* probes, ui
     return 0;
 }
 
+// The reference's B+tree page layout (src/btree.cuh:30-64) for uint64 keys
+// and values: page size, header size, offsets of the separators and of the
+// child pointers within an inner page, separators per inner node, keys per
+// leaf.
+void ref_btree_layout(uint64_t out[6]) {
+    using tree_t = index_structures::btree<uint64_t, uint64_t, host_alloc, ~0ull>;
+    out[0] = tree_t::page_size;
+    out[1] = sizeof(tree_t::NodeBase);
+    out[2] = __builtin_offsetof(tree_t::InnerNode, keys);
+    out[3] = __builtin_offsetof(tree_t::InnerNode, children);
+    out[4] = tree_t::InnerNode::maxEntries;
+    out[5] = tree_t::LeafNode::maxEntries;
+}
+
+// The reference's host-built B+tree (load factor 1.0) as a canonical word
+// stream, breadth first from the root: per inner node its count, its
+// isFinalInner flag and its count separators, and for a final inner node
+// its count + 1 children as column positions.  Writes at most cap words;
+// returns the stream's length.
+uint64_t ref_btree_canonical(const uint64_t* col, uint64_t n, uint64_t* out, uint64_t cap) {
+    using tree_t = index_structures::btree<uint64_t, uint64_t, host_alloc, ~0ull>;
+    if (n == 0) return 0;
+    std::vector<uint64_t> keys(col, col + n);
+    quiet_cout q;
+    tree_t tree;
+    tree.construct(keys, 1.0f);
+    uint64_t len = 0;
+    auto put = [&](uint64_t w) {
+        if (len < cap) out[len] = w;
+        ++len;
+    };
+    std::vector<const tree_t::InnerNode*> level{static_cast<const tree_t::InnerNode*>(tree.root)};
+    while (!level.empty()) {
+        std::vector<const tree_t::InnerNode*> next;
+        for (const tree_t::InnerNode* nd : level) {
+            put(nd->header.count);
+            put(nd->header.isFinalInner ? 1 : 0);
+            for (unsigned i = 0; i < nd->header.count; ++i) put(nd->keys[i]);
+            for (unsigned i = 0; i <= nd->header.count; ++i) {
+                if (nd->header.isFinalInner)
+                    put(static_cast<uint64_t>(static_cast<const uint64_t*>(nd->children[i]) - keys.data()));
+                else
+                    next.push_back(static_cast<const tree_t::InnerNode*>(nd->children[i]));
+            }
+        }
+        level.swap(next);
+    }
+    return len;
+}
+
 // Harmonia with 32 keys per node (fanout 33, src/indexes.cuh:264), host
 // lookup src/harmonia.cuh:640-668.  Returns 1 if construct() throws.
 int ref_harmonia_lookup_u64(const uint64_t* col, uint64_t n, const uint64_t* probes, uint64_t m,

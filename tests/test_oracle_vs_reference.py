@@ -33,6 +33,23 @@ def test_btree_random_sizes(ref, n):
     np.testing.assert_array_equal(ref.BTree(col).lookup(pr), ref.ref_btree_lookup(col, pr))
 
 
+@pytest.mark.parametrize("n", [1, 247, 248, 247 * 246, 247 * 246 + 1, 247 * 247 * 3 + 5, 1000003])
+def test_btree_page_image_is_the_reference_tree(ref, n):
+    # The page image that the GPU timing of the reference's own B+tree lookup
+    # runs on (oracle/ref_gpu.py) is the oracle's build written in the
+    # reference's page layout; read back breadth first it must be the tree
+    # the reference's btree::construct builds: the same nodes, counts, final
+    # flags, separators and leaf positions.
+    rng = np.random.default_rng(n + 3)
+    col = np.unique(rng.integers(0, 1 << 62, size=n + 64, dtype=np.uint64))[:n]
+    page, header, keys_off, children_off, inner_keys, leaf_keys = ref.ref_btree_layout()
+    assert (page, header, inner_keys, leaf_keys) == (4096, 128, 246, 247)
+    pages_base, col_base = 0x7F0000000000, 0x7E0000000000
+    image, root = ref.BTree(col, leaf_keys, inner_keys).pages(page, keys_off, children_off, pages_base, col_base)
+    ours = ref.btree_canonical_from_pages(image, page, keys_off, children_off, root, pages_base, col_base)
+    np.testing.assert_array_equal(ours, ref.ref_btree_canonical(col))
+
+
 @pytest.mark.parametrize("n", [2, 3, 5, 1000, 65537])
 def test_search_random_sizes(ref, n):
     rng = np.random.default_rng(n + 11)
