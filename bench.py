@@ -201,9 +201,11 @@ def time_steps(fn, steps: int, warmup: int, stream, world: int, device):
 
 def reference_gpu_lookup(ref, kind, ix, keys, h_keys, probes, out, expect, steps, warmup, stream, world, device):
     """Times the reference's own device lookup of `kind` (oracle/ref_gpu.py:
-    its binary_search_index / harmonia_tree lookups compiled from its headers)
-    and this library's lookup (gj_index_lookup, the same u32 positions) on the
-    same index data and probes; both outputs are compared with the oracle's
+    its binary_search_index / btree / harmonia_tree lookups compiled from its
+    headers) and this library's lookup (gj_index_lookup, the same u32
+    positions; for binary search and Harmonia also the warp-collective
+    gj_index_lookup_cooperative with the reference's 16-lane groups) on the
+    same index data and probes; every output is compared with the oracle's
     positions."""
     import torch
 
@@ -222,7 +224,11 @@ def reference_gpu_lookup(ref, kind, ix, keys, h_keys, probes, out, expect, steps
     else:
         run_ref = lambda: ref.binary_search(keys, probes, out, stream)  # noqa: E731
     res = {}
-    for arm, fn in (("reference_kernel", run_ref), ("gb300_lookup", lambda: ix.lookup(probes, out=out))):
+    arms = [("reference_kernel", run_ref), ("gb300_lookup", lambda: ix.lookup(probes, out=out))]
+    if kind in ("harmonia", "binary_search"):
+        # the same warp-collective protocol as the reference's (16-lane groups)
+        arms.append(("gb300_warp_cooperative_16", lambda: ix.lookup_cooperative(probes, 4, out=out)))
+    for arm, fn in arms:
         out.fill_(0)
         ms = max_over_ranks(time_steps(fn, steps, warmup, stream, world, device), world, device)
         mism = None
@@ -479,9 +485,17 @@ def north_star_extras(args, world, device, stream, keys, h_keys, h_probes):
     num, den = oracle.star_join(h[0].view(np.uint32), h[1].view(np.uint32), h[2], h[3], h[4].view(np.uint64), h[5],
                                 lo, hi)
     cpu_s = time.perf_counter() - c0
+    sout2 = torch.zeros(2, dtype=torch.int64, device=device)
+    ms_sorted = time_steps(lambda: gj.star_join_sum(six, fk, date, price, disc, flag, lo, hi, sout2,
+                                                    sorted_batches=True), steps, args.warmup, stream, world, device)
+    got2 = sout2.cpu().numpy()
     extras["star"] = {"fact_rows_per_s": n_fact * steps / (ms / 1e3), "latency_us": ms / steps * 1e3,
                       "sums": [int(got[0]), int(got[1])], "oracle_sums": [num, den],
                       "exact": bool(int(got[0]) == num and int(got[1]) == den),
+                      "sorted_batches": {"fact_rows_per_s": n_fact * steps / (ms_sorted / 1e3),
+                                         "latency_us": ms_sorted / steps * 1e3,
+                                         "exact": bool(int(got2[0]) == num and int(got2[1]) == den),
+                                         "order": "gj_star_join_sum_sorted (ij_pbws: buffered, key-sorted batches)"},
                       "cpu_query_14_part_build_1_thread_rows_per_s": n_fact / cpu_s,
                       "config": "6M fact rows, 200k dimension rows (B+tree), 30-day window of 2556 days"}
     six.free()
@@ -727,7 +741,7 @@ def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind
     import gpujoin_gb300 as gj
 
     n, m = 1 << n_log2, 1 << m_log2
-    keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << 63, seed=args.seed)
+    keys = gj.generate_sorted_keys(n, gj.DIST_UNIFORM, 1 << args.key_bits, seed=args.seed)
     probes = gj.generate_probes(keys, m, theta=args.theta, seed=args.seed + 1)
     pairs = torch.empty(2 * m, dtype=torch.int32, device=device)
     count = torch.zeros(1, dtype=torch.int64, device=device)
@@ -787,6 +801,19 @@ def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind
                         "frac": round(achieved / peak, 4), "bytes_per_probe": bpp,
                         "peak_source": f"{peak_kind} hbm_gbs (copy, burst)"},
            "launches_per_step": 3 + ((m + window - 1) // window) * 8, "clocks": clocks}
+    # The probe pass reads its index slices from L2 (a partition's directory
+    # and column slice stay resident while its probes run), one random
+    # 32-byte sector per request; so its floor is the L2 rate of random
+    # sector reads (calibrated here over a 32 MB buffer) times the L2 read
+    # requests per probe that ncu counts (profiles/traffic.txt).
+    if not args.no_calibration and n_log2 >= 24:
+        req = profile_traffic(f"l2_read_requests_per_probe_k_part_probe_n{n_log2}")
+        cal = random_sector_rate(device, stream, n_sectors=1 << 20, loads=1 << 28, reps=3)
+        rate = cal["default_fill"]["sectors_per_s"]
+        out["probe_l2_floor"] = {"l2_random_sectors_per_s": round(rate / 1e9, 1), "unit": "G sectors/s",
+                                 "calibration_buffer_bytes": cal["buffer_bytes"],
+                                 "l2_read_requests_per_probe": req,
+                                 "probe_ms_floor": round(req * m / rate * 1e3, 3) if req else None}
     ix.free()
     del keys, probes, pairs, ws, pws
     torch.cuda.empty_cache()
@@ -1280,6 +1307,8 @@ def parse_args(argv=None):
     ap.add_argument("--btree-leaf-keys", type=int, default=0, help="B+tree leaf width (0 = library default)")
     ap.add_argument("--learned-leaves", type=int, default=0, help="learned: leaf models (0 = library default)")
     ap.add_argument("--radix-bits", type=int, default=0, help="partitioned: fanout bits (0 = autotune)")
+    ap.add_argument("--key-bits", type=int, default=63,
+                    help="partitioned: build keys drawn from [0, 2^bits) (default 63, the INLJ configuration)")
     ap.add_argument("--window", type=int, default=0, help="partitioned: window size in probes (0 = autotune)")
     ap.add_argument("--parity-sample", type=int, default=1 << 25,
                     help="probe rows checked against the oracle where not every probe is checked")

@@ -142,6 +142,7 @@ _SIGNATURES = {
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
     "gj_index_key_range": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
+    "gj_index_lookup_cooperative": (_i32, [_vp, _vp, _u64, _vp, _u32, _vp]),
     "gj_partition_shift": (_i32, [_u64, _u64, _u32, ctypes.POINTER(_u32)]),
     "gj_range_partition": (_i32, [_vp, _u64, _u64, _u32, _u32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gj_partitioned_lookup": (_i32, [_vp, _vp, _vp, _u64, _vp, _vp]),
@@ -154,6 +155,7 @@ _SIGNATURES = {
     "gj_tpch_q14": (_i32, [ctypes.POINTER(gj_q14_tables), _vp, ctypes.POINTER(ctypes.c_int64),
                            ctypes.POINTER(ctypes.c_double)]),
     "gj_star_join_sum": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
+    "gj_star_join_sum_sorted": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _u32, _u32, _vp, _vp]),
     "gj_learned_mlp_grad": (_i32, [_vp, _u32, _vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_autotune_partitioned": (_i32, [_vp, _vp, _u64, _vp, ctypes.POINTER(_u32), ctypes.POINTER(_u64),
                                        ctypes.POINTER(ctypes.c_float)]),
@@ -354,6 +356,17 @@ class abstract_index:
         _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
                                    _ptr(workspace), workspace.numel(), _stream(stream)))
         return out_pairs, out_count
+
+    def lookup_cooperative(self, d_probes, degree=4, out=None, stream=None):
+        """lookup() through the warp-collective search (groups of 2**degree lanes;
+        cooperative_binary_search / harmonia_tree::lookup<Degree>): binary search and Harmonia."""
+        torch = _torch()
+        m = d_probes.numel()
+        if out is None:
+            out = _empty(m, torch.int32, d_probes.device)
+        _check(lib().gj_index_lookup_cooperative(self.handle, _ptr(d_probes), m, _ptr(out), int(degree),
+                                                 _stream(stream)))
+        return out
 
     def lookup_sorted(self, d_probes, out=None, stream=None):
         """Block-wise sorted lookup (bws_lookup, src/index_lookup_common.cuh:398-549): the positions of lookup()."""
@@ -636,13 +649,15 @@ def tpch_q14(lineitem_tbl: str, part_tbl: str, stream=None):
 
 
 def star_join_sum(dim_index: abstract_index, d_fk, d_date, d_price, d_discount, d_dim_flag, lo: int, hi: int,
-                  out=None, stream=None):
-    """Returns a 2-element int64 tensor [sum over flagged rows, sum over all rows]."""
+                  out=None, stream=None, sorted_batches: bool = False):
+    """Returns a 2-element int64 tensor [sum over flagged rows, sum over all rows].
+    sorted_batches: the reference's pipelined ij_pbws order (gj_star_join_sum_sorted)."""
     torch = _torch()
     if out is None:
         out = torch.zeros(2, dtype=torch.int64, device=d_fk.device)
-    _check(lib().gj_star_join_sum(dim_index.handle, _ptr(d_fk), _ptr(d_date), _ptr(d_price), _ptr(d_discount),
-                                  d_fk.numel(), _ptr(d_dim_flag), lo, hi, _ptr(out), _stream(stream)))
+    fn = lib().gj_star_join_sum_sorted if sorted_batches else lib().gj_star_join_sum
+    _check(fn(dim_index.handle, _ptr(d_fk), _ptr(d_date), _ptr(d_price), _ptr(d_discount), d_fk.numel(),
+              _ptr(d_dim_flag), lo, hi, _ptr(out), _stream(stream)))
     return out
 
 

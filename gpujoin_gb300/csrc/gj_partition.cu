@@ -221,6 +221,12 @@ size_t scatter_smem_bytes(uint32_t fanout) {
 #define GJ_WIDE_RADIX_BITS 8
 #endif
 constexpr uint32_t kWideRadixBits = GJ_WIDE_RADIX_BITS;
+// the sorted tile keeps each key's partition beside its offset (one 32-bit
+// word), so the write pass reads it instead of recomputing it from the key
+// (1); GJ_SCATTER_META=0 recomputes it
+#ifndef GJ_SCATTER_META
+#define GJ_SCATTER_META 1
+#endif
 constexpr int kWideBlock = 1024;
 constexpr int kWideItems = 8;
 constexpr uint32_t kWideTile = kWideBlock * kWideItems;
@@ -236,7 +242,11 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_dst + fanout);     // fanout
     uint32_t* s_start = s_cnt + fanout;                                // fanout
     unsigned long long* s_delta = reinterpret_cast<unsigned long long*>(s_start + fanout);  // fanout
+#if GJ_SCATTER_META
+    uint32_t* s_meta = reinterpret_cast<uint32_t*>(s_delta + fanout);  // kWideTile: partition << 16 | offset
+#else
     uint16_t* s_off = reinterpret_cast<uint16_t*>(s_delta + fanout);   // kWideTile
+#endif
     for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) {
         const uint64_t cell = (uint64_t)p * gridDim.x + blockIdx.x;
         s_dst[p] = cell == 0 ? 0ull : incl[cell - 1];
@@ -245,7 +255,7 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
     const unsigned long long* k64 = reinterpret_cast<const unsigned long long*>(keys);
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
     static_assert(kWideTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
-    static_assert(kWideTile <= (1u << 16), "16-bit tile offsets");
+    static_assert(kWideTile <= (1u << 16) && (1u << kMaxRadixBits) <= (1u << 16), "16-bit tile offsets and partitions");
     uint64_t next[kWideItems];
 #pragma unroll
     for (int k = 0; k < kWideItems; ++k) {
@@ -280,7 +290,11 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
             if (j < tn) {
                 const uint32_t q = s_start[slot[k] >> 13] + (slot[k] & ((1u << 13) - 1));
                 s_keys[q] = key[k];
+#if GJ_SCATTER_META
+                s_meta[q] = ((slot[k] >> 13) << 16) | j;
+#else
                 s_off[q] = (uint16_t)j;
+#endif
             }
         }
         // output index of the tile's j-th sorted key = s_delta[p] + j
@@ -288,9 +302,17 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < tn; j += kWideBlock) {
             const uint64_t k = s_keys[j];
+#if GJ_SCATTER_META
+            // the partition and the tile offset were stored with the key
+            const uint32_t meta = s_meta[j];
+            const uint64_t d = s_delta[meta >> 16] + j;
+            __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
+            __stcg(out_rows + d, (uint32_t)(row_base + t0 + (meta & 0xFFFFu)));
+#else
             const uint64_t d = s_delta[part_of(k, min_key, shift, fanout)] + j;
             __stcg(reinterpret_cast<unsigned long long*>(out_keys) + d, (unsigned long long)k);
             __stcg(out_rows + d, (uint32_t)(row_base + t0 + s_off[j]));
+#endif
         }
         __syncthreads();
         for (uint32_t p = threadIdx.x; p < fanout; p += kWideBlock) {
@@ -302,7 +324,8 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
 }
 
 size_t scatter_wide_smem_bytes(uint32_t fanout) {
-    return (size_t)kWideTile * (sizeof(uint64_t) + sizeof(uint16_t)) + (size_t)fanout * (8 + 4 + 4 + 8);
+    return (size_t)kWideTile * (sizeof(uint64_t) + (GJ_SCATTER_META ? sizeof(uint32_t) : sizeof(uint16_t))) +
+           (size_t)fanout * (8 + 4 + 4 + 8);
 }
 
 struct partition_plan {

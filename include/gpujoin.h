@@ -179,6 +179,18 @@ int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ---- warp-collective searches ---------------------------------------------- */
+/* gj_index_lookup with the reference's warp-collective search protocol:
+ * groups of 2^degree lanes (degree 1..5) serve their members' probes one
+ * after another, one round of loads per step -- cooperative_binary_search
+ * (src/search.cuh:355-386) for a binary-search index, harmonia_tree::
+ * lookup<Degree> (src/harmonia.cuh:740-786) for a Harmonia index.  Results
+ * equal gj_index_lookup's; other index kinds return GJ_ERR_UNSUPPORTED.
+ * The per-thread gj_index_lookup is the faster form for independent probes
+ * (a warp keeps 32 searches in flight instead of 32 / 2^degree). */
+int gj_index_lookup_cooperative(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_positions,
+                                uint32_t degree, void* stream);
+
 /* ---- block-wise sorted probe order ---------------------------------------- */
 /* bws_lookup (src/index_lookup_common.cuh:398-549): each tile of 1024 probes
  * is sorted by key in shared memory and searched in that order, so lanes of
@@ -315,6 +327,13 @@ int gj_partitioned_inlj(const gj_index* index, const uint64_t* d_probes, uint64_
 int gj_star_join_sum(const gj_index* dim_index, const uint32_t* d_fk, const uint32_t* d_date,
                      const int64_t* d_price, const int64_t* d_discount, uint64_t nfact,
                      const uint8_t* d_dim_flag, uint32_t lo, uint32_t hi, int64_t* d_out, void* stream);
+/* The same sums in the reference's pipelined order, ij_pbws
+ * (src/tpch/tpch_14_ij.cu:95-362): the rows that pass the date filter are
+ * buffered per block across tiles, sorted by foreign key in batches of 2048
+ * and probed in key order.  nfact < 2^32. */
+int gj_star_join_sum_sorted(const gj_index* dim_index, const uint32_t* d_fk, const uint32_t* d_date,
+                            const int64_t* d_price, const int64_t* d_discount, uint64_t nfact,
+                            const uint8_t* d_dim_flag, uint32_t lo, uint32_t hi, int64_t* d_out, void* stream);
 
 /* ---- TPC-H Q14 from dbgen .tbl files -------------------------------------- */
 /* The columns of Q14 (load_tables_with_aria_parser, src/tpch/common.cpp:

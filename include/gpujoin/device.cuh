@@ -5,8 +5,10 @@
 // functions are what the library's own kernels run; reference-style kernels
 // call them through the device_index_t wrappers in gpujoin/indexes.cuh.
 //
-// All lookups are per-thread (no warp-collective requirement); results
-// follow the reference's per-index semantics:
+// All lookups are per-thread (no warp-collective requirement), except the
+// warp-cooperative searches near the end of this file, which mirror the
+// reference's cooperative entry points; results follow the reference's
+// per-index semantics:
 //   binary search / radix spline / learned: lower bound, GJ_INVALID_POS at n
 //   B+tree / Harmonia: position of an equal key, else GJ_INVALID_POS.
 //
@@ -669,6 +671,112 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
     const uint64_t p =
         lower_bound_sectors<kColumn>(v.col, v.n, leaf_first, leaf_first + K, key, v.col_aligned, &eq);
     return eq ? (uint32_t)p : kInvalid;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative searches: the counterparts of the reference's
+// cooperative_binary_search (src/search.cuh:296-386) and
+// harmonia_tree::lookup<Degree> (src/harmonia.cuh:740-786).  Groups of
+// 2^kDegree lanes serve their members' queries one after another; every
+// round each lane of the group loads one key (or one 2^(5-kDegree)-key slice
+// of a Harmonia node) and a ballot or a reduction combines them.  All 32
+// lanes of the warp must call together, converged; inactive lanes only lend
+// their loads.  Results equal the per-thread searches'.  For a stream of
+// independent probes the per-thread searches are the faster form on GB300 (a
+// warp keeps 32 searches in flight instead of 32 / 2^kDegree); these serve
+// code written against the reference's cooperative calls.
+// ---------------------------------------------------------------------------
+GJ_DEVICE_INLINE uint32_t lane_index() {
+    uint32_t l;
+    asm("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+template <unsigned kDegree>
+GJ_DEVICE_INLINE uint32_t group_mask_of(uint32_t first) {
+    return kDegree >= 5 ? 0xffffffffu : (((1u << (1u << kDegree)) - 1u) << first);
+}
+
+// Lower bound of x in arr[0, size) (size if every key is below x) by a
+// (G + 1)-ary search, G = 2^kDegree: each round the G lanes test the G
+// pivots lo + (i + 1) * len / (G + 1) of the candidate range [lo, hi], and
+// the number of pivots below x selects one of the G + 1 parts (the keys are
+// sorted, so the tests below x are a prefix of the lanes); a range of at most
+// G positions is finished in one last round.  log_{G+1}(size) + 1 rounds.
+template <unsigned kDegree = 4>
+GJ_DEVICE_INLINE uint64_t cooperative_lower_bound(bool active, uint64_t x, const uint64_t* arr, uint64_t size) {
+    static_assert(kDegree >= 1 && kDegree <= 5, "groups of 2 to 32 lanes");
+    constexpr uint32_t G = 1u << kDegree;
+    const uint32_t lane = lane_index();
+    const uint32_t first = lane & ~(G - 1u), me = lane - first;
+    const uint32_t mask = group_mask_of<kDegree>(first);
+    uint64_t result = size;
+    for (uint32_t s = 0; s < G; ++s) {
+        const uint32_t leader = first + s;
+        if (!__shfl_sync(mask, active ? 1 : 0, leader)) continue;  // the same answer on every lane of the group
+        const uint64_t lx = __shfl_sync(mask, (unsigned long long)x, leader);
+        const uint64_t* la =
+            reinterpret_cast<const uint64_t*>(__shfl_sync(mask, (unsigned long long)(uintptr_t)arr, leader));
+        uint64_t lo = 0, hi = __shfl_sync(mask, (unsigned long long)size, leader);
+        while (hi - lo > G) {
+            // the answer lies in [lo, hi]; pivot i = lo + (i + 1) * len / (G + 1)
+            const uint64_t len = hi - lo, lo0 = lo;
+            const uint64_t p = lo0 + (uint64_t)(me + 1) * len / (G + 1);
+            const uint32_t below = __popc(__ballot_sync(mask, ld_ro(la + p) < lx));
+            // pivots 0 .. below - 1 are below x, pivot `below` (if any) is not
+            if (below > 0) lo = lo0 + (uint64_t)below * len / (G + 1) + 1;
+            if (below < G) hi = lo0 + (uint64_t)(below + 1) * len / (G + 1);
+        }
+        const uint64_t p = lo + me;
+        const uint32_t below = __popc(__ballot_sync(mask, p < hi && ld_ro(la + p) < lx));
+        if (lane == leader) result = lo + below;
+    }
+    return active ? result : size;
+}
+
+// Harmonia lookup (exact match, as harmonia_lookup) with a group of
+// 2^kDegree lanes per node: each lane reads a 32 / 2^kDegree-key slice of the
+// 32-key node and the group sums the counts of keys below the probe (the
+// node's lower bound, one round of loads per level instead of about three
+// dependent sector loads).
+template <unsigned kDegree = 4>
+GJ_DEVICE_INLINE uint32_t harmonia_lookup_cooperative(bool active, const harmonia_view& v, uint64_t key) {
+    static_assert(kDegree >= 1 && kDegree <= 5, "groups of 2 to 32 lanes");
+    constexpr uint32_t G = 1u << kDegree, kSlice = kHarmoniaKeys / G;
+    const uint32_t lane = lane_index();
+    const uint32_t first = lane & ~(G - 1u), me = lane - first;
+    const uint32_t mask = group_mask_of<kDegree>(first);
+    uint32_t result = kInvalid;
+    for (uint32_t s = 0; s < G; ++s) {
+        const uint32_t leader = first + s;
+        if (!__shfl_sync(mask, active ? 1 : 0, leader)) continue;
+        const uint64_t lx = __shfl_sync(mask, (unsigned long long)key, leader);
+        uint64_t pos = 0;
+        for (uint32_t d = 1; d < v.depth; ++d) {
+            const uint64_t* node = v.keys + pos * kHarmoniaKeys + me * kSlice;
+            uint32_t c = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < kSlice; ++j) c += ld_ro(node + j) < lx ? 1u : 0u;
+            const uint32_t lb = __reduce_add_sync(mask, c);
+            pos = ld_ro(v.children + pos) + lb;
+        }
+        // leaf level: node pos covers column [32 * pos - inner_size, +32)
+        const uint64_t leaf_first = (v.depth > 1) ? (pos * kHarmoniaKeys - v.inner_size) : 0;
+        const uint64_t* leaf = v.col + leaf_first + me * kSlice;
+        uint32_t c = 0;
+        bool eq = false;
+#pragma unroll
+        for (uint32_t j = 0; j < kSlice; ++j) {
+            const bool in = leaf_first + me * kSlice + j < v.n;
+            const uint64_t k = in ? ld_ro(leaf + j) : ~0ull;
+            c += in && k < lx ? 1u : 0u;
+            eq |= in && k == lx;
+        }
+        const uint32_t lb = __reduce_add_sync(mask, c);
+        const bool found = __ballot_sync(mask, eq) != 0;
+        if (lane == leader && found) result = (uint32_t)(leaf_first + lb);
+    }
+    return active ? result : kInvalid;
 }
 
 // ---------------------------------------------------------------------------

@@ -13,6 +13,10 @@
 // key for btree / harmonia, invalid for no_op) and returns
 // numeric_limits<Value>::max() where the reference returns invalid_tid.  It
 // does not need the whole warp: lanes may call it independently.
+// binary_search_index and harmonia_index also offer
+// warp_cooperative_lookup<Degree>(active, key), the reference's
+// warp-collective protocol (groups of 2^Degree lanes per query, the whole
+// warp calling), with the same results.
 //
 // Keys must be uint64 (the reference's index_key_t, src/index_lookup_config.hpp:45).
 // The allocator template parameters are accepted for source compatibility;
@@ -162,6 +166,13 @@ struct harmonia_index : public gj::detail::index_base<GJ_INDEX_HARMONIA, gj::har
         __device__ __forceinline__ value_t cooperative_lookup(const bool active, const key_t key) const {
             return active ? gj::detail::to_tid<value_t>(gj::harmonia_lookup(v, nullptr, key)) : invalid_tid;
         }
+        // harmonia_tree::lookup<Degree> (src/harmonia.cuh:740-786): groups of
+        // 2^Degree lanes per node; the whole warp calls it, converged
+        template <unsigned Degree = 4>
+        __device__ __forceinline__ value_t warp_cooperative_lookup(const bool active, const key_t key) const {
+            const uint32_t r = gj::harmonia_lookup_cooperative<Degree>(active, v, key);
+            return active ? gj::detail::to_tid<value_t>(r) : invalid_tid;
+        }
     } device_index;
 
     void construct(const vector_view<key_t>& h_column, const key_t* d_column) override {
@@ -180,6 +191,13 @@ struct binary_search_index : public gj::detail::index_base<GJ_INDEX_BINARY_SEARC
         gj::bs_view v;
         __device__ __forceinline__ value_t cooperative_lookup(const bool active, const key_t key) const {
             return active ? gj::detail::to_tid<value_t>(gj::bs_lookup(v, v.fence, key)) : invalid_tid;
+        }
+        // cooperative_binary_search (src/search.cuh:355-386): groups of
+        // 2^Degree lanes per query; the whole warp calls it, converged
+        template <unsigned Degree = 4>
+        __device__ __forceinline__ value_t warp_cooperative_lookup(const bool active, const key_t key) const {
+            const uint64_t r = gj::cooperative_lower_bound<Degree>(active, key, v.col, v.n);
+            return active && r < v.n ? static_cast<value_t>(r) : invalid_tid;
         }
     } device_index;
 

@@ -30,6 +30,55 @@ __global__ void probe_all(const IndexStructureType index_structure, uint64_t n, 
     }
 }
 
+// the reference's lookup_kernel with a warp-collective lookup: every lane
+// of a warp reaches the call, inactive ones with active = false
+template <class IndexStructureType, unsigned Degree>
+__global__ void probe_all_warp(const IndexStructureType index_structure, uint64_t n,
+                               const index_key_t* __restrict__ keys, value_t* __restrict__ tids) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t limit = (n + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < limit; i += stride) {
+        const bool active = i < n;
+        const index_key_t key = active ? keys[i] : 0;
+        const value_t tid = index_structure.template warp_cooperative_lookup<Degree>(active, key);
+        if (active) tids[i] = tid;
+    }
+}
+
+template <class IndexType, unsigned Degree>
+static int run_warp(const index_key_t* d_col, const index_key_t* h_col, uint64_t n, const index_key_t* d_keys,
+                    uint64_t m, value_t* d_tids) {
+    IndexType index;
+    index.construct(vector_view<index_key_t>(const_cast<index_key_t*>(h_col), n), d_col);
+    const int block = 128;
+    const uint64_t blocks = (m + block - 1) / block;
+    probe_all_warp<typename IndexType::device_index_t, Degree>
+        <<<(unsigned)(blocks ? (blocks < 65535 ? blocks : 65535) : 1), block>>>(index.device_index, m, d_keys, d_tids);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : 2;
+}
+
+// warp-collective lookups: kind 1 = harmonia, 2 = binary_search; degree 1..5
+extern "C" int drop_in_probe_warp(int kind, int degree, const index_key_t* d_col, const index_key_t* h_col,
+                                  uint64_t n, const index_key_t* d_keys, uint64_t m, value_t* d_tids) {
+    try {
+        using H = harmonia_index<index_key_t, value_t>;
+        using B = binary_search_index<index_key_t, value_t>;
+        switch (kind * 10 + degree) {
+            case 11: return run_warp<H, 1>(d_col, h_col, n, d_keys, m, d_tids);
+            case 12: return run_warp<H, 2>(d_col, h_col, n, d_keys, m, d_tids);
+            case 14: return run_warp<H, 4>(d_col, h_col, n, d_keys, m, d_tids);
+            case 15: return run_warp<H, 5>(d_col, h_col, n, d_keys, m, d_tids);
+            case 21: return run_warp<B, 1>(d_col, h_col, n, d_keys, m, d_tids);
+            case 22: return run_warp<B, 2>(d_col, h_col, n, d_keys, m, d_tids);
+            case 24: return run_warp<B, 4>(d_col, h_col, n, d_keys, m, d_tids);
+            case 25: return run_warp<B, 5>(d_col, h_col, n, d_keys, m, d_tids);
+            default: return 3;
+        }
+    } catch (const std::exception&) {
+        return 1;
+    }
+}
+
 template <class IndexType>
 static int run(const index_key_t* d_col, const index_key_t* h_col, uint64_t n, const index_key_t* d_keys,
                uint64_t m, value_t* d_tids) {

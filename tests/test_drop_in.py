@@ -66,6 +66,34 @@ def test_reference_style_code_probes(tmp_path, orc, gj, cuda, kind, name):
     np.testing.assert_array_equal(got, exp64)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,name", [(1, "harmonia"), (2, "binary_search")])
+@pytest.mark.parametrize("degree", [1, 2, 4, 5])
+def test_reference_style_warp_cooperative_lookup(tmp_path, orc, gj, cuda, kind, name, degree):
+    # warp_cooperative_lookup<Degree>: the reference's warp-collective
+    # protocol (groups of 2^Degree lanes per query, every lane of the warp
+    # calling, a partly inactive last warp) with the per-thread results
+    import torch
+
+    lib = ctypes.CDLL(build_drop_in(tmp_path))
+    lib.drop_in_probe_warp.restype = ctypes.c_int
+    lib.drop_in_probe_warp.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                       ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    rng = np.random.default_rng(10 * kind + degree)
+    col = np.sort(np.unique(rng.integers(0, 1 << 63, 80000, dtype=np.uint64)))[: 32 * 2000]
+    pr = np.concatenate([col[rng.integers(0, len(col), 20000)], rng.integers(0, 1 << 63, 5001, dtype=np.uint64),
+                         np.array([0, col[0], col[-1], col[-1] + 1, (1 << 64) - 1], dtype=np.uint64)])
+    d_col = torch.from_numpy(col.view(np.int64)).cuda()
+    d_pr = torch.from_numpy(pr.view(np.int64)).cuda()
+    out = torch.empty(len(pr), dtype=torch.int64, device="cuda")
+    rc = lib.drop_in_probe_warp(kind, degree, d_col.data_ptr(), col.ctypes.data, len(col), d_pr.data_ptr(), len(pr),
+                                out.data_ptr())
+    assert rc == 0
+    exp = orc.exact_lookup(col, pr) if name == "harmonia" else orc.bs_lookup(col, pr)
+    exp64 = np.where(exp == 0xFFFFFFFF, np.uint64(0xFFFFFFFFFFFFFFFF), exp.astype(np.uint64))
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint64), exp64)
+
+
 def _parse(lib, args):
     argv = (ctypes.c_char_p * (len(args) + 1))(b"index_lookup", *[a.encode() for a in args])
     out = (ctypes.c_uint64 * 10)()

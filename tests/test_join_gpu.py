@@ -162,9 +162,10 @@ def star_inputs(rng, nfact, ndim):
     return dim, flag, fk, date, price, disc
 
 
+@pytest.mark.parametrize("sorted_batches", [False, True])
 @pytest.mark.parametrize("kind", ["btree", "harmonia", "binary_search", "radix_spline"])
 @pytest.mark.parametrize("nfact", [0, 1, 4095, 4097, 600000])
-def test_star_join_matches_oracle(orc, gj, cuda, kind, nfact):
+def test_star_join_matches_oracle(orc, gj, cuda, kind, nfact, sorted_batches):
     import torch
 
     rng = np.random.default_rng(nfact + 1)
@@ -175,7 +176,8 @@ def test_star_join_matches_oracle(orc, gj, cuda, kind, nfact):
     ix = gj.make_index(kind).construct(None, to_dev(torch, dim))
     t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()
     out = gj.star_join_sum(ix, t(fk.view(np.int32), torch.int32), t(date.view(np.int32), torch.int32),
-                           t(price, torch.int64), t(disc, torch.int64), t(flag, torch.uint8), lo, hi)
+                           t(price, torch.int64), t(disc, torch.int64), t(flag, torch.uint8), lo, hi,
+                           sorted_batches=sorted_batches)
     num, den = orc.star_join(fk, date, price, disc, dim, flag, lo, hi)
     got = out.cpu().numpy()
     assert int(got[0]) == num and int(got[1]) == den
@@ -190,10 +192,11 @@ def test_star_join_full_window_and_empty_window(orc, gj, cuda):
     t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()
     args = (t(fk.view(np.int32), torch.int32), t(date.view(np.int32), torch.int32), t(price, torch.int64),
             t(disc, torch.int64), t(flag, torch.uint8))
-    for lo, hi in ((0, 1 << 31), (500, 500), (2555, 2556)):
-        got = gj.star_join_sum(ix, *args, lo, hi).cpu().numpy()
+    for lo, hi in ((0, 1 << 31), (500, 500), (2555, 2556), (100, 900)):
         num, den = orc.star_join(fk, date, price, disc, dim, flag, lo, hi)
-        assert (int(got[0]), int(got[1])) == (num, den)
+        for sorted_batches in (False, True):  # every row passes / none / a few / a third
+            got = gj.star_join_sum(ix, *args, lo, hi, sorted_batches=sorted_batches).cpu().numpy()
+            assert (int(got[0]), int(got[1])) == (num, den), (lo, hi, sorted_batches)
 
 
 @pytest.mark.parametrize("kind", ["btree", "radix_spline", "learned"])

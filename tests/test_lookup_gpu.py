@@ -320,3 +320,33 @@ def test_hash_index_edge_keys(orc, gj, cuda):
         assert ix.memory_consumption() >= 16 * 2 * len(col)
         got = from_dev_u32(ix.lookup(to_dev(torch, pr)))
         np.testing.assert_array_equal(got, orc.exact_lookup(col, pr), err_msg=name)
+
+
+@pytest.mark.parametrize("kind", ["harmonia", "binary_search"])
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5])
+def test_warp_cooperative_lookup(orc, gj, cuda, kind, degree):
+    # gj_index_lookup_cooperative: the reference's warp-collective protocol
+    # (groups of 2^degree lanes), the per-thread results; ragged probe counts
+    # leave the last warp partly inactive
+    import torch
+
+    rng = np.random.default_rng(degree)
+    for n in (32, 4096, 1 << 18):
+        col = column(rng, n)
+        pr = probes_for(rng, col, 30001)
+        ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+        got = from_dev_u32(ix.lookup_cooperative(to_dev(torch, pr), degree))
+        np.testing.assert_array_equal(got, expected(orc, kind, col, pr), err_msg=f"n={n}")
+        ix.free()
+
+
+def test_warp_cooperative_lookup_rejects_other_kinds(gj, cuda):
+    import torch
+
+    keys = gj.generate_sorted_keys(1 << 10, gj.DIST_UNIFORM, 1 << 63, seed=3)
+    ix = gj.make_index("btree").construct(None, keys)
+    with pytest.raises(gj.GJError):
+        ix.lookup_cooperative(keys[:10], 4)
+    ix2 = gj.make_index("harmonia").construct(None, keys)
+    with pytest.raises(gj.GJError):
+        ix2.lookup_cooperative(keys[:10], 6)

@@ -2,8 +2,9 @@
 the oracle: a column whose keys crowd into a few buckets (long lower-bound
 ranges, searched past the first sectors), a column that is not 32-byte
 aligned, columns of a few keys, clustered keys with long gaps (buckets
-filled by the prefix maximum), probes outside the key range, several
-windows, and the directory built per call or kept with the index.
+filled by the prefix maximum), narrower key ranges, a run of consecutive
+keys, probes outside the key range, several windows, and the directory
+built per call or kept with the index.
 Positions must equal the oracle's per probe row, the pairs as a set (their
 order across tiles is not fixed)."""
 import numpy as np
@@ -29,12 +30,21 @@ def _column(case, rng):
         return np.unique(col)
     if case == "tiny":
         return np.array([5, 17, 1 << 40, (1 << 64) - 2, (1 << 64) - 1], dtype=np.uint64)
+    # narrower key ranges (directory buckets a few keys wide), and a run of
+    # 3000 consecutive keys inside one bucket among sparse ones
+    if case == "range48":
+        return column(rng, 100_003, upper=1 << 48)
+    if case == "range52":
+        return column(rng, 1 << 17, upper=1 << 52)
+    if case == "run":
+        col = column(rng, 1 << 17, upper=1 << 49)
+        return np.unique(np.concatenate([col, np.arange(1 << 40, (1 << 40) + 3000, dtype=np.uint64)]))
     return column(rng, 100_003)  # "unaligned" and "plain"
 
 
 @pytest.mark.parametrize("prepared", [False, True])
 @pytest.mark.parametrize("kind", KINDS)
-@pytest.mark.parametrize("case", ["wide", "unaligned", "tiny", "clusters"])
+@pytest.mark.parametrize("case", ["wide", "unaligned", "tiny", "clusters", "range48", "range52", "run"])
 def test_partitioned_directory_cases(orc, gj, cuda, kind, case, prepared):
     import torch
 
