@@ -221,14 +221,14 @@ def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m):
     np.testing.assert_array_equal(got[:, 1], epos)
 
 
-def test_inlj_pairs_host_buffers_large(orc, gj, cuda):
-    # 2^24 + 54321 probes from host buffers: every pair in probe order, the
-    # status reads clean
+@pytest.mark.parametrize("m", [(1 << 24) + 54321, 3 * (1 << 24) + 5])
+def test_inlj_pairs_host_buffers_large(orc, gj, cuda, m):
+    # tens of millions of probes from host buffers: every pair in probe
+    # order, the status reads clean
     import torch
 
     rng = np.random.default_rng(3)
     col = column(rng, 1 << 16)
-    m = (1 << 24) + 54321
     pr = col[rng.integers(0, len(col), m)]
     pr[::7] = pr[::7] + np.uint64(1)  # some absent keys
     ix = gj.btree_index().construct(None, to_dev(torch, col))
