@@ -95,6 +95,17 @@ __global__ void k_btree_start(btree_view v, uint64_t entries, uint64_t* __restri
     }
 }
 
+// start table of a Harmonia tree: entry b = the deepest node shared by the
+// descents of every key of bucket b (the bucket's first and last key)
+__global__ void k_harmonia_start(harmonia_view v, uint64_t max_key, uint64_t entries, uint64_t* __restrict__ out) {
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < entries;
+         b += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = v.min_key + (b << v.start_shift);
+        const uint64_t hi = b + 1 == entries ? max_key : lo + ((1ull << v.start_shift) - 1);
+        out[b] = harmonia_common_node(v, lo, hi);
+    }
+}
+
 // B+tree level l, W separators per node, fanout F = W + 1: slot k = (node j,
 // separator c) is the max key of child j*F + c one level down, which covers
 // the column range [child * span, (child + 1) * span); UINT64_MAX past the end
@@ -467,6 +478,43 @@ int build_harmonia(gj_index* idx, const uint64_t* h_keys, cudaStream_t s) {
     idx->hm.cached_levels = cached_levels;
     idx->hm.col_aligned = aligned32(idx->d_col);
     idx->bytes = (ha.keys.size() + ha.children.size()) * sizeof(uint64_t);
+
+    // start table, as for the B+tree (one bucket per about 64 keys, 2^1 ..
+    // 2^20 buckets, btree_start_bits to override): most buckets then lie
+    // inside one node above the leaves, or one leaf node, and a lookup
+    // starts there instead of at the root
+    const uint64_t n = idx->n;
+    uint32_t R = idx->params.btree_start_bits;
+    if (R > 24) {
+        set_error("harmonia: start table bits must be at most 24");
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (R == 0) {
+        R = 1;
+        while (R < 20 && (n >> (R + 7)) != 0) ++R;
+    }
+    const uint64_t min_key = col[0], max_key = col[n - 1];
+    const uint64_t range = max_key - min_key;
+    const uint32_t used = range ? 64u - (uint32_t)__builtin_clzll(range) : 0u;
+    const uint32_t shift = used > R ? used - R : 0u;
+    const uint64_t entries = (range >> shift) + 1;
+    void* tp = nullptr;
+    GJ_TRY(device_alloc(idx, entries * sizeof(uint64_t), &tp));
+    harmonia_view tv = idx->hm;
+    tv.cached_nodes = 0;
+    tv.cached_levels = 0;
+    tv.min_key = min_key;
+    tv.start = nullptr;
+    tv.start_shift = shift;
+    const int grid = (int)std::min<uint64_t>((entries + 255) / 256, 4096);
+    k_harmonia_start<<<grid, 256, 0, s>>>(tv, max_key, entries, static_cast<uint64_t*>(tp));
+    GJ_CUDA_TRY(cudaGetLastError());
+    GJ_CUDA_TRY(cudaStreamSynchronize(s));
+    idx->hm.min_key = min_key;
+    idx->hm.start = static_cast<const uint64_t*>(tp);
+    idx->hm.start_shift = shift;
+    idx->hm.start_entries = (uint32_t)entries;
+    idx->bytes += entries * sizeof(uint64_t);
     return GJ_OK;
 }
 

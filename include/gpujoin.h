@@ -98,8 +98,8 @@ typedef struct gj_index_params {
     uint32_t index_memory;      /* where the index's own arrays live: GJ_INDEX_MEMORY_DEVICE (HBM, default)
                                    or GJ_INDEX_MEMORY_HOST (pinned Grace memory, read by the kernels over
                                    NVLink-C2C; pair it with a column in pinned host memory) */
-    uint32_t btree_start_bits;  /* B+tree start table: the key range cut into 2^bits buckets, each mapped to
-                                   the deepest node its keys share, where scattered lookups start (default 0:
+    uint32_t btree_start_bits;  /* B+tree and Harmonia start table: the key range cut into 2^bits buckets, each
+                                   mapped to the deepest node its keys share, where lookups start (default 0:
                                    about one bucket per 64 keys, at most 2^20; 1..24 as given) */
     uint64_t seed;              /* training / sampling seed */
 } gj_index_params;

@@ -636,6 +636,14 @@ struct harmonia_view {
     uint32_t cached_nodes;   // leading nodes (level order) staged in shared memory
     uint32_t cached_levels;  // the cached nodes are exactly the top cached_levels levels
     uint32_t col_aligned;    // column base is 32-byte aligned
+    // start table: the key range [min_key, max key] cut into buckets of
+    // 2^start_shift keys; entry b (8 bytes: node | level << 56) is the
+    // deepest node every key of bucket b passes, where a lookup starts its
+    // descent (null: from the root)
+    uint64_t min_key;
+    const uint64_t* start;
+    uint32_t start_shift;
+    uint32_t start_entries;
 };
 
 // Shared cache layout: cached_nodes * 32 keys, then cached_nodes children.
@@ -647,8 +655,18 @@ GJ_DEVICE_INLINE uint32_t harmonia_lookup(const harmonia_view& v, const uint64_t
     constexpr int kColumn = kScattered ? kL2Stream : kL2Default;
     constexpr uint32_t K = kHarmoniaKeys;
     uint64_t pos = 0;
+    uint32_t d0 = 1;
     const uint32_t depth = v.depth;
-    for (uint32_t d = 1; d < depth; ++d) {
+    if (v.start != nullptr && key >= v.min_key) {
+        // one 8-byte load in place of the levels above the bucket's node
+        const uint64_t b = (key - v.min_key) >> v.start_shift;
+        if (b < v.start_entries) {
+            const uint64_t e = ld_ro_c<kInner>(v.start + b);
+            pos = e & ((1ull << 56) - 1);
+            d0 = (uint32_t)(e >> 56);
+        }
+    }
+    for (uint32_t d = d0; d < depth; ++d) {
         uint32_t lb;
         uint64_t child;
         if (d <= v.cached_levels) {
@@ -732,6 +750,25 @@ GJ_DEVICE_INLINE uint64_t cooperative_lower_bound(bool active, uint64_t x, const
         if (lane == leader) result = lo + below;
     }
     return active ? result : size;
+}
+
+// Where the descents of lo and hi (lo <= hi) part: the deepest node both
+// pass, as (node | level << 56) -- level d means the node is searched at
+// loop level d, depth means it is the leaf node.  Every key in [lo, hi]
+// passes through it (the descent is monotonic in the key).
+GJ_DEVICE_INLINE uint64_t harmonia_common_node(const harmonia_view& v, uint64_t lo, uint64_t hi) {
+    constexpr uint32_t K = kHarmoniaKeys;
+    uint64_t pos = 0;
+    uint32_t d = 1;
+    for (; d < v.depth; ++d) {
+        bool eq;
+        const uint64_t* node = v.keys + pos * K;
+        const uint32_t a = (uint32_t)lower_bound_sectors(node, K, 0, K, lo, true, &eq);
+        const uint32_t b = (uint32_t)lower_bound_sectors(node, K, 0, K, hi, true, &eq);
+        if (a != b) break;
+        pos = ld_ro(v.children + pos) + a;
+    }
+    return pos | ((uint64_t)d << 56);
 }
 
 // Harmonia lookup (exact match, as harmonia_lookup) with a group of

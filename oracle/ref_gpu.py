@@ -24,7 +24,9 @@ BLOCK = 128  # the reference's default block size (src/index_lookup_config.hpp:2
 class HarmoniaView(ctypes.Structure):
     """gj::harmonia_view (include/gpujoin/device.cuh) as gj_index_device_view writes it."""
     _fields_ = [(f, ctypes.c_uint64) for f in ("keys", "children", "col", "n", "inner_size")] + \
-               [(f, ctypes.c_uint32) for f in ("depth", "cached_nodes", "cached_levels", "col_aligned")]
+               [(f, ctypes.c_uint32) for f in ("depth", "cached_nodes", "cached_levels", "col_aligned")] + \
+               [(f, ctypes.c_uint64) for f in ("min_key", "start")] + \
+               [(f, ctypes.c_uint32) for f in ("start_shift", "start_entries")]
 
 
 def available() -> bool:
