@@ -328,6 +328,8 @@ def index_params(args, kind):
             p["btree_leaf_keys"] = args.btree_leaf_keys
         if args.btree_start_bits:
             p["btree_start_bits"] = args.btree_start_bits
+    if kind == "harmonia" and args.btree_start_bits:
+        p["btree_start_bits"] = args.btree_start_bits  # Harmonia's start table shares the parameter
     return p
 
 
