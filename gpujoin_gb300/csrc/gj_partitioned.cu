@@ -10,11 +10,11 @@
 //
 // Directory.  For probes that arrive grouped by key range, the inner levels
 // of a tree are replaced by a flat radix directory over the column: the key
-// range [min, max] of the index cut into 2^B equal buckets (about two per
+// range [min, max] of the index cut into 2^B equal buckets (about four per
 // 32-byte column sector), and per bucket the sector that holds the lower
 // bound of the bucket's first key (u32).  The lower bound of a probe key in
 // bucket g then lies in the sectors named by entries g and g + 1 -- for
-// uniform keys one or two sectors (99.6 %), rarely a third.  The probe reads
+// uniform keys mostly the first, else the next, rarely a third.  The probe reads
 // the two entries (one 32-byte sector of the directory, mostly) and the
 // column sector(s): two dependent loads, both L2 hits because the probes of a
 // partition touch one slice of the directory and the column, which stay in
@@ -254,10 +254,10 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
             // kProbeBatch probes of the thread go through each phase
             // together, so that their loads are in flight at the same time:
             // directory entries; the sector of the first entry (the lower
-            // bound lies there for 75 % of uniform keys at two buckets per
-            // sector); the next sector when the range goes on (99.6 % by
-            // then); anything else (a longer range, a partial last sector, an
-            // unaligned column) takes the sector binary search.
+            // bound lies there for about 7 in 8 uniform keys at four buckets
+            // per sector); the next sector when the range goes on; anything
+            // else (a longer range, a partial last sector, an unaligned
+            // column) takes the sector binary search.
             uint64_t key[kProbeBatch];
             uint32_t slo[kProbeBatch], shi[kProbeBatch];
             bool todo[kProbeBatch];
@@ -427,11 +427,18 @@ int semantics_of(const gj_index* idx) {
     }
 }
 
-// directory buckets: about two per 32-byte sector of the column (2^B >= n / 2)
+// directory buckets: about four per 32-byte sector of the column (2^B >= n):
+// 10.64 against 10.90 ms per 2^29 probes into 2^28 keys with two per sector
+// (the second sector is needed less often), 12.27 with one.
+// GJ_DIR_BITS_DELTA (tuning builds) shifts it by powers of two
+#ifndef GJ_DIR_BITS_DELTA
+#define GJ_DIR_BITS_DELTA 1
+#endif
 uint32_t dir_bits_for(uint64_t n) {
     uint32_t b = 4;
     while (b < kMaxDirBits && (1ull << b) < n / 2) ++b;
-    return b;
+    const int d = (int)b + GJ_DIR_BITS_DELTA;
+    return d < 4 ? 4u : d > (int)kMaxDirBits ? kMaxDirBits : (uint32_t)d;
 }
 
 struct partitioned_layout {

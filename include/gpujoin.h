@@ -308,7 +308,7 @@ int gj_partitioned_lookup(const gj_index* index, const uint64_t* d_part_keys, co
 int gj_partitioned_inlj_workspace_size(const gj_index* index, uint64_t window_size, uint32_t radix_bits,
                                        size_t* bytes);
 /* Builds the index's partition directory (the radix table over its column
- * that gj_partitioned_inlj probes through, about 2 bytes per key) and keeps
+ * that gj_partitioned_inlj probes through, about 4 bytes per key) and keeps
  * it with the index, like the B+tree's start table; later partitioned calls
  * skip building it and need less workspace.  Synchronous; idempotent.  No
  * counterpart in the reference. */
