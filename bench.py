@@ -816,6 +816,20 @@ def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind
                                  "calibration_buffer_bytes": cal["buffer_bytes"],
                                  "l2_read_requests_per_probe": req,
                                  "probe_ms_floor": round(req * m / rate * 1e3, 3) if req else None}
+        # The step against the roofline of what bounds each of its parts:
+        # the partition passes stream 8 + 20 B per probe at HBM peak; the
+        # probe pass needs its L2 random-sector reads (above) or its 12 + 8 B
+        # per probe of streaming at HBM peak, whichever takes longer.
+        if req:
+            part_ms = 28.0 * m / (peak * 1e9) * 1e3
+            probe_ms = max(req * m / rate * 1e3, 20.0 * m / (peak * 1e9) * 1e3)
+            floor = part_ms + probe_ms
+            out["roofline_sector"] = {
+                "bound": "hbm (histogram + scatter) + L2 random 32-byte sectors (probe pass)",
+                "floor_ms": round(floor, 3), "partition_ms_floor": round(part_ms, 3),
+                "probe_ms_floor": round(probe_ms, 3), "achieved_ms": round(per_step, 3),
+                "frac": round(floor / per_step, 4),
+                "peaks": f"{peak_kind} hbm_gbs {peak} GB/s; L2 random sectors {rate / 1e9:.1f} G/s (calibrated now)"}
     ix.free()
     del keys, probes, pairs, ws, pws
     torch.cuda.empty_cache()
