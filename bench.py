@@ -1035,7 +1035,9 @@ def star_workload(args, world, rank, device, stream):
     dim_keys, flag, fk, date, price, disc = star_inputs(n_fact, n_dim, args.seed, device)
     ix = gj.btree_index().construct(None, dim_keys)
     out = torch.zeros(2, dtype=torch.int64, device=device)
-    ms = time_steps(lambda: gj.star_join_sum(ix, fk, date, price, disc, flag, lo, hi, out), args.steps, args.warmup,
+    sorted_batches = args.star_order == "sorted"
+    ms = time_steps(lambda: gj.star_join_sum(ix, fk, date, price, disc, flag, lo, hi, out,
+                                             sorted_batches=sorted_batches), args.steps, args.warmup,
                     stream, world, device)
     ms = max_over_ranks(ms, world, device)
     got = out.cpu().numpy()
@@ -1049,7 +1051,8 @@ def star_workload(args, world, rank, device, stream):
     return _base_line(
         args, world, "star-join fact rows/s (1 GB300 per rank)", world * n_fact * args.steps / (ms / 1e3),
         "fact rows/s", per_step,
-        f"star join: {n_fact} fact rows, {n_dim} dimension rows (B+tree), 30-day window of 2556 days",
+        f"star join: {n_fact} fact rows, {n_dim} dimension rows (B+tree), 30-day window of 2556 days"
+        + (", rows buffered and probed in key-sorted batches" if sorted_batches else ""),
         {"star": {"sums": [int(got[0]), int(got[1])], "oracle_sums": [num, den],
                   "exact": bool(int(got[0]) == num and int(got[1]) == den), "latency_us": per_step * 1e3},
          "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -1332,6 +1335,8 @@ def parse_args(argv=None):
                     help="learned: only binary search, RadixSpline and the learned builds at both leaf counts")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks (timing runs)")
     ap.add_argument("--no-calibration", action="store_true", help="inlj: skip the random-sector calibration")
+    ap.add_argument("--star-order", choices=["probe", "sorted"], default="probe",
+                    help="star: fact-row order of the lookups (sorted = buffered, key-sorted batches)")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="inlj: skip timing the reference's own device lookups (oracle/_ref/refgpu.cubin)")
     ap.add_argument("--no-extras", action="store_true",
