@@ -62,7 +62,16 @@ constexpr uint32_t kScanTile = kScanBlock * kScanPer;
 #define GJ_PROBE_SPECULATE 0
 #endif
 constexpr int kProbeBlock = 256;
-constexpr int kProbeBatch = 2;             // probes per thread searched together (loads in flight)
+// probes per thread searched together (loads in flight) and resident
+// blocks per SM (the register cap); GJ_PROBE_BATCH / GJ_PROBE_BLOCKS override
+// them in tuning builds
+#ifndef GJ_PROBE_BATCH
+#define GJ_PROBE_BATCH 2
+#endif
+#ifndef GJ_PROBE_BLOCKS
+#define GJ_PROBE_BLOCKS 3
+#endif
+constexpr int kProbeBatch = GJ_PROBE_BATCH;
 constexpr int kProbeItems = 8;             // probes per thread and tile (one atomicAdd per tile)
 constexpr uint32_t kProbeTile = kProbeBlock * kProbeItems;
 constexpr uint32_t kChunk = 4 * kProbeTile;  // probes per block
@@ -232,7 +241,7 @@ struct probe_args {
 };
 
 template <int kSem, bool kAligned>
-__global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_constant__ probe_args a) {
+__global__ void __launch_bounds__(kProbeBlock, GJ_PROBE_BLOCKS) k_part_probe(const __grid_constant__ probe_args a) {
     constexpr int kWarps = kProbeBlock / 32;
     __shared__ uint32_t s_cnt[kWarps * kProbeItems];
     __shared__ unsigned long long s_base;
@@ -413,6 +422,7 @@ __global__ void __launch_bounds__(kProbeBlock, 3) k_part_probe(const __grid_cons
     }
 }
 static_assert(kProbeBlock / 32 * kProbeItems % 32 == 0, "the tile scan gives each lane whole counts");
+static_assert(kProbeItems % kProbeBatch == 0, "whole batches per tile");
 
 // ---------------------------------------------------------------------------
 // host side
