@@ -73,3 +73,34 @@ def test_partitioned_directory_cases(orc, gj, cuda, kind, case, prepared):
         order = np.argsort(a[:, 0], kind="stable")
         np.testing.assert_array_equal(a[order, 0], erows, err_msg=f"{kind}/{case}/2^{bits}")
         np.testing.assert_array_equal(a[order, 1], epos, err_msg=f"{kind}/{case}/2^{bits}")
+
+
+@pytest.mark.parametrize("kind", ["btree", "binary_search"])
+def test_partitioned_skewed_probes(orc, gj, cuda, kind):
+    # Nearly every probe falls into one narrow key range (one partition, a
+    # few directory buckets), every 64th into the lowest keys, some are
+    # absent: one partition far fuller than the others, across windows.
+    import torch
+
+    rng = np.random.default_rng(77)
+    col = column(rng, 1 << 18)
+    m = 300_000
+    hot = col[(1 << 17):(1 << 17) + 512]
+    pr = hot[rng.integers(0, len(hot), m)]
+    pr[::64] = col[rng.integers(0, 64, len(pr[::64]))]
+    pr[::97] = pr[::97] + np.uint64(1)  # some absent keys
+    ix = gj.make_index(kind).construct(None, to_dev(torch, col))
+    exp = expected(orc, kind, col, pr)
+    erows, epos = orc.pairs_from_positions(exp)
+    for prepared in (False, True):
+        if prepared:
+            ix.prepare_partitioned()
+        for bits, window in ((8, 0), (11, 0), (8, 65536)):
+            pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=bits,
+                                                positions=True, pairs=True)
+            np.testing.assert_array_equal(from_dev_u32(pos), exp, err_msg=f"{kind}/2^{bits}/{window}")
+            c = int(cnt.item())
+            a = prs[: 2 * c].cpu().numpy().view(np.uint32).reshape(-1, 2)
+            order = np.argsort(a[:, 0], kind="stable")
+            np.testing.assert_array_equal(a[order, 0], erows)
+            np.testing.assert_array_equal(a[order, 1], epos)
