@@ -1065,12 +1065,12 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
     """Learned index against binary search and RadixSpline at exact outputs:
     2^27 keys from three distributions, 2^28 uniformly sampled probes with 5%
     absent keys, lower-bound positions.  The learned index runs as its
-    default build (column-sized leaves, root chosen per column) and at the
-    configuration's 2^14 leaves (root chosen per column, and the 2x32 MLP
-    root alone); RadixSpline at its default error 32 and at the learned
-    model's recorded error bound.  Every index's positions are compared with
-    the oracle on a seeded sample of probe rows plus every absent key, and
-    in full with the GPU binary search."""
+    default build (column-sized leaves, root chosen per column), at 2^14
+    leaves (root chosen per column, and the 2x32 MLP root alone) and at 2^16
+    leaves (the top of the 2^12-2^16 range); RadixSpline at its default error
+    32 and at each learned model's recorded error bound.  Every index's
+    positions are compared with the oracle on a seeded sample of probe rows
+    plus every absent key, and in full with the GPU binary search."""
     import numpy as np
     import torch
 
@@ -1085,11 +1085,12 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
                ("learned", "learned", dict(leaves)),
                ("learned_2^14_leaves", "learned", {"learned_leaves": 1 << 14}),
                ("learned_mlp_2^14_leaves", "learned", {"learned_root": gj.LEARNED_ROOT_MLP, "learned_leaves": 1 << 14}),
+               ("learned_2^16_leaves", "learned", {"learned_leaves": 1 << 16}),
                ("learned_mlp", "learned", {"learned_root": gj.LEARNED_ROOT_MLP, **leaves}),
                ("learned_segments", "learned", {"learned_root": gj.LEARNED_ROOT_SEGMENTS, **leaves}),
                ("learned_linear", "learned", {"learned_root": gj.LEARNED_ROOT_LINEAR, **leaves}))
     if quick:
-        configs = configs[:5]
+        configs = configs[:6]
     parity_total = {"checked": 0, "mismatches": 0}
     for dist_name, dist in (("uniform", gj.DIST_UNIFORM), ("lognormal", gj.DIST_LOGNORMAL),
                             ("clusters", gj.DIST_CLUSTERS)):
@@ -1134,7 +1135,8 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
             row[name] = entry
             ix.free()
         # RadixSpline at the learned models' recorded error bounds (equal epsilon)
-        for lname in ("learned", "learned_2^14_leaves"):
+        lnames = [n for n in ("learned", "learned_2^14_leaves", "learned_2^16_leaves") if n in row]
+        for lname in lnames:
             eps = int(min(row[lname]["max_error"], (1 << 31) - 1))
             ix = gj.radix_spline_index(rs_max_error=max(eps, 1)).construct(None, keys)
             ms = time_steps(lambda: ix.lookup(probes, out), steps, args.warmup, stream, world, device)
@@ -1143,7 +1145,7 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
             judge(entry)
             row[f"radix_spline_eps_of_{lname}"] = entry
             ix.free()
-        for lname in ("learned", "learned_2^14_leaves"):
+        for lname in lnames:
             row[f"{lname}_beats"] = {k: row[lname]["tuples_per_s"] > row[k]["tuples_per_s"]
                                      for k in ("binary_search", "radix_spline", f"radix_spline_eps_of_{lname}")}
         results[dist_name] = row
