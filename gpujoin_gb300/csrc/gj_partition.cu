@@ -227,11 +227,27 @@ constexpr uint32_t kWideRadixBits = GJ_WIDE_RADIX_BITS;
 #ifndef GJ_SCATTER_META
 #define GJ_SCATTER_META 1
 #endif
-constexpr int kWideBlock = 1024;
+// block size, resident blocks per SM and the register prefetch of the next
+// tile (one 1024-thread block with the prefetch measured fastest: 10.63 ms
+// per partitioned step of 2^29 probes, against 11.71 for two 1024-thread
+// blocks without it and 11.18 / 12.47 for two 768-thread blocks without /
+// with it); GJ_WIDE_BLOCK / GJ_WIDE_PER_SM / GJ_WIDE_PREFETCH override them
+// in tuning builds
+#ifndef GJ_WIDE_BLOCK
+#define GJ_WIDE_BLOCK 1024
+#endif
+#ifndef GJ_WIDE_PER_SM
+#define GJ_WIDE_PER_SM 1
+#endif
+#ifndef GJ_WIDE_PREFETCH
+#define GJ_WIDE_PREFETCH 1
+#endif
+constexpr int kWideBlock = GJ_WIDE_BLOCK;
+constexpr int kWidePerSM = GJ_WIDE_PER_SM;
 constexpr int kWideItems = 8;
 constexpr uint32_t kWideTile = kWideBlock * kWideItems;
 
-__global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint64_t* __restrict__ keys, uint64_t m,
+__global__ void __launch_bounds__(kWideBlock, kWidePerSM) k_part_scatter_wide(const uint64_t* __restrict__ keys, uint64_t m,
                                                                      uint64_t chunk, uint64_t min_key, uint32_t shift,
                                                                      uint32_t fanout, const uint64_t* __restrict__ incl,
                                                                      uint64_t row_base, uint64_t* __restrict__ out_keys,
@@ -256,16 +272,19 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
     const uint64_t b0 = blockIdx.x * chunk, b1 = min(m, b0 + chunk);
     static_assert(kWideTile <= (1u << 13) && (1u << kMaxRadixBits) <= (1u << 19), "slot packing");
     static_assert(kWideTile <= (1u << 16) && (1u << kMaxRadixBits) <= (1u << 16), "16-bit tile offsets and partitions");
+#if GJ_WIDE_PREFETCH
     uint64_t next[kWideItems];
 #pragma unroll
     for (int k = 0; k < kWideItems; ++k) {
         const uint64_t i = b0 + (uint64_t)k * kWideBlock + threadIdx.x;
         next[k] = i < b1 ? __ldcs(k64 + i) : 0ull;
     }
+#endif
     __syncthreads();
     for (uint64_t t0 = b0; t0 < b1; t0 += kWideTile) {
         const uint32_t tn = b1 - t0 < kWideTile ? (uint32_t)(b1 - t0) : kWideTile;
         uint64_t key[kWideItems];
+#if GJ_WIDE_PREFETCH
 #pragma unroll
         for (int k = 0; k < kWideItems; ++k) key[k] = next[k];
         const uint64_t t1 = t0 + kWideTile;
@@ -274,6 +293,13 @@ __global__ void __launch_bounds__(kWideBlock, 1) k_part_scatter_wide(const uint6
             const uint64_t i = t1 + (uint64_t)k * kWideBlock + threadIdx.x;
             next[k] = i < b1 ? __ldcs(k64 + i) : 0ull;
         }
+#else
+#pragma unroll
+        for (int k = 0; k < kWideItems; ++k) {
+            const uint64_t i = t0 + (uint64_t)k * kWideBlock + threadIdx.x;
+            key[k] = i < b1 ? __ldcs(k64 + i) : 0ull;
+        }
+#endif
         uint32_t slot[kWideItems];  // partition << 13 | rank inside the tile's partition run
 #pragma unroll
         for (int k = 0; k < kWideItems; ++k) {
@@ -339,7 +365,7 @@ partition_plan plan_partition(uint64_t m, uint32_t radix_bits, int sm_count) {
     pl.fanout = 1u << radix_bits;
     pl.wide = radix_bits >= kWideRadixBits;
     // the scatter kernel's resident blocks
-    uint64_t nb = (uint64_t)sm_count * (pl.wide ? 1 : kScatterPerSM);
+    uint64_t nb = (uint64_t)sm_count * (pl.wide ? kWidePerSM : kScatterPerSM);
     const uint64_t min_chunk = 4096;
     if (nb * min_chunk > m) nb = std::max<uint64_t>(1, (m + min_chunk - 1) / min_chunk);
     pl.chunk = (m + nb - 1) / nb;
@@ -386,7 +412,8 @@ int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, u
                                              (int)smem_scatter));
     }
     if (pl.wide)
-        k_part_hist<1024><<<pl.nblocks, 1024, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift, pl.fanout, hist);
+        k_part_hist<kWideBlock><<<pl.nblocks, kWideBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift,
+                                                                          pl.fanout, hist);
     else
         k_part_hist<kPartBlock><<<pl.nblocks, kPartBlock, smem_hist, s>>>(d_keys, m, pl.chunk, min_key, shift,
                                                                           pl.fanout, hist);
