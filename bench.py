@@ -424,7 +424,8 @@ def cpu_baselines(h_keys, h_probes, one_sample, all_sample):
 def other_configurations(args, world, device, stream, keys, h_keys, h_probes):
     """The other configurations of the INLJ measurement, each checked against
     the oracle: the same B+tree at Zipf theta 0 and 1.0; the partitioned INLJ
-    of 2^29 Zipf(0.5) probes into a 2^28-key index (autotuned fanout); the
+    of 2^29 Zipf(0.5) probes into a 2^28-key index (autotuned fanout), and on
+    the headline's 2^26 keys and 2^28 probes; the
     learned index against binary search and RadixSpline (2^27 keys x three
     distributions, 2^28 probes with 5% absent keys); the star-join aggregate;
     and the reference's CPU lookup paths at 1 and all host threads."""
@@ -467,6 +468,14 @@ def other_configurations(args, world, device, stream, keys, h_keys, h_probes):
     t0 = time.perf_counter()
     extras["partitioned"] = partitioned_measure(args, world, device, stream, 28, 29, steps, "btree")
     extras["partitioned"]["seconds"] = round(time.perf_counter() - t0, 1)
+
+    # the partitioned INLJ on the headline's data (2^26 keys, 2^28 Zipf(0.5)
+    # probes): the same set of pairs as the headline, grouped by partition
+    # tile instead of in probe order
+    t0 = time.perf_counter()
+    extras["partitioned_headline_data"] = partitioned_measure(args, world, device, stream, 26, 28, steps, "btree",
+                                                              sample_clocks=False)
+    extras["partitioned_headline_data"]["seconds"] = round(time.perf_counter() - t0, 1)
 
     t0 = time.perf_counter()
     results, parity = learned_measure(args, world, device, stream, 27, 28, 3, quick=True)
@@ -964,8 +973,10 @@ def host_index_workload(args, world, rank, device, stream):
 def orderings_workload(args, world, rank, device, stream):
     """Probe order as an autotuner choice (the reference's block-wise sorted
     lookups, src/index_lookup_common.cuh:398-549): INLJ pairs of 2^m_log2
-    probes into 2^n_log2 keys in probe order and from sorted tiles, over
-    Zipf theta 0 (uniform), 0.5 and 1.0, with the autotuner's pick."""
+    probes into 2^n_log2 keys in probe order, from sorted tiles and
+    range-partitioned (one window, default fanout, directory kept with the
+    index), over Zipf theta 0 (uniform), 0.5 and 1.0, with the autotuner's
+    pick."""
     import ctypes
 
     import torch
@@ -981,18 +992,29 @@ def orderings_workload(args, world, rank, device, stream):
     wsz = ctypes.c_size_t(0)
     gj.lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(wsz))
     ws = torch.empty(wsz.value, dtype=torch.uint8, device=device)
+    ix.prepare_partitioned()
+    pwsz = ctypes.c_size_t(0)
+    gj._check(gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, m, 0, ctypes.byref(pwsz)))
+    pws = torch.empty(pwsz.value, dtype=torch.uint8, device=device)
+
+    def partitioned(probes, pairs, count, ws):
+        gj._check(gj.lib().gj_partitioned_inlj(ix.handle, probes.data_ptr(), m, m, 0, None, pairs.data_ptr(),
+                                                count.data_ptr(), pws.data_ptr(), pws.numel(), stream.cuda_stream))
+
+    names = {gj.ORDER_PROBE: "probe", gj.ORDER_SORTED_TILES: "sorted_tiles", gj.ORDER_PARTITIONED: "partitioned"}
     thetas, head = {}, None
     for theta in (0.0, 0.5, 1.0):
         probes = gj.generate_probes(keys, m, theta=theta, seed=args.seed + 1)
         row = {}
-        for name, fn in (("probe", ix.inlj_pairs), ("sorted_tiles", ix.inlj_pairs_sorted)):
+        for name, fn in (("probe", ix.inlj_pairs), ("sorted_tiles", ix.inlj_pairs_sorted),
+                         ("partitioned", partitioned)):
             ms = time_steps(lambda: fn(probes, pairs, count, ws), args.steps, args.warmup, stream, world, device)
             ms = max_over_ranks(ms, world, device)
             row[name] = {"tuples_per_s": world * m * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                          "pairs": int(count.item())}
         pick, _ = ix.autotune_ordering(probes)
-        row["autotune"] = "sorted_tiles" if pick == gj.ORDER_SORTED_TILES else "probe"
-        row["same_pairs"] = row["probe"]["pairs"] == row["sorted_tiles"]["pairs"]
+        row["autotune"] = names[pick]
+        row["same_pairs"] = row["probe"]["pairs"] == row["sorted_tiles"]["pairs"] == row["partitioned"]["pairs"]
         thetas[str(theta)] = row
         if theta == args.theta:
             head = row
@@ -1003,7 +1025,7 @@ def orderings_workload(args, world, rank, device, stream):
         args, world, f"INLJ probe tuples/s ({kind}, autotuned probe order, 1 GB300 per rank)", best["tuples_per_s"],
         "probe tuples/s", best["ms_per_step"],
         f"INLJ pairs: {n} uniform uint64 build keys, {m} Zipf probes (theta 0, 0.5, 1.0), probe order vs "
-        f"block-wise sorted tiles of 1024",
+        f"block-wise sorted tiles of 1024 vs range-partitioned",
         {"orderings": {"index": kind, "thetas": thetas}, "gpu_launches": None, "cpu_baseline": None, "e2e": None})
 
 

@@ -90,6 +90,7 @@ class gj_index_params(ctypes.Structure):
 # probe orders (gj_autotune_ordering)
 ORDER_PROBE = 0
 ORDER_SORTED_TILES = 1
+ORDER_PARTITIONED = 2
 
 # gj_index_params.index_memory
 INDEX_MEMORY_DEVICE = 0
@@ -395,7 +396,8 @@ class abstract_index:
         return out_pairs, out_count
 
     def autotune_ordering(self, d_probes, stream=None):
-        """(ORDER_PROBE or ORDER_SORTED_TILES, best ms) for pairs of these probes."""
+        """(ORDER_PROBE, ORDER_SORTED_TILES or ORDER_PARTITIONED, best ms) for
+        pairs of these probes."""
         o, ms = _u32(0), ctypes.c_float(0)
         _check(lib().gj_autotune_ordering(self.handle, _ptr(d_probes), d_probes.numel(), _stream(stream),
                                           ctypes.byref(o), ctypes.byref(ms)))

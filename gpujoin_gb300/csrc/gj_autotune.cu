@@ -174,7 +174,25 @@ int gj_autotune_ordering(const gj_index* index, const uint64_t* d_probes, uint64
         },
         s, 2, ev, &t_sorted));
     *ordering = t_sorted < t_probe ? GJ_ORDER_SORTED_TILES : GJ_ORDER_PROBE;
-    if (best_ms) *best_ms = t_sorted < t_probe ? t_sorted : t_probe;
+    float best = t_sorted < t_probe ? t_sorted : t_probe;
+    // the partitioned INLJ in one window at the default fanout, timed as the
+    // index stands (an index without its kept directory builds it per call)
+    size_t pws_bytes = 0;
+    GJ_TRY(gj_partitioned_inlj_workspace_size(index, m, 0, &pws_bytes));
+    device_buffer pws;
+    GJ_TRY(pws.alloc(pws_bytes));
+    float t_part = 0.f;
+    GJ_TRY(time_best(
+        [&] {
+            return gj_partitioned_inlj(index, d_probes, m, m, 0, nullptr, static_cast<uint32_t*>(pairs.p),
+                                       static_cast<uint64_t*>(count.p), pws.p, pws_bytes, stream);
+        },
+        s, 2, ev, &t_part));
+    if (t_part < best) {
+        *ordering = GJ_ORDER_PARTITIONED;
+        best = t_part;
+    }
+    if (best_ms) *best_ms = best;
     return GJ_OK;
 }
 

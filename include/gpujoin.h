@@ -204,7 +204,13 @@ int gj_inlj_pairs_sorted(const gj_index* index, const uint64_t* d_probes, uint64
                          uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 #define GJ_ORDER_PROBE 0u        /* gj_inlj_pairs */
 #define GJ_ORDER_SORTED_TILES 1u /* gj_inlj_pairs_sorted */
-/* the faster probe order for these probes (pairs), timed on the caller's data */
+#define GJ_ORDER_PARTITIONED 2u  /* gj_partitioned_inlj, one window, default fanout */
+/* the fastest probe order for these probes (pairs), timed on the caller's
+ * data: probe order, sorted tiles, or range-partitioned (the pairs of
+ * gj_partitioned_inlj: the same set, grouped by partition tile; timed as the
+ * index stands, so an index not prepared with gj_index_prepare_partitioned
+ * pays for building the directory each call).  Allocates the workspaces it
+ * times with. */
 int gj_autotune_ordering(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
                          uint32_t* ordering, float* best_ms);
 

@@ -61,11 +61,14 @@ def test_autotune_ordering(orc, gj, cuda):
     d_pr = to_dev(torch, pr)
     ix = gj.btree_index().construct(None, to_dev(torch, col))
     order, ms = ix.autotune_ordering(d_pr)
-    assert order in (gj.ORDER_PROBE, gj.ORDER_SORTED_TILES) and ms > 0
-    run = ix.inlj_pairs_sorted if order == gj.ORDER_SORTED_TILES else ix.inlj_pairs
-    out, cnt = run(d_pr)
-    rows, pos = pairs_of(out, cnt)
+    assert order in (gj.ORDER_PROBE, gj.ORDER_SORTED_TILES, gj.ORDER_PARTITIONED) and ms > 0
     erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
-    order_ = np.argsort(rows, kind="stable")
-    np.testing.assert_array_equal(rows[order_], erows)
-    np.testing.assert_array_equal(pos[order_], epos)
+    # every candidate order gives the same set of pairs
+    runs = {gj.ORDER_PROBE: lambda: ix.inlj_pairs(d_pr), gj.ORDER_SORTED_TILES: lambda: ix.inlj_pairs_sorted(d_pr),
+            gj.ORDER_PARTITIONED: lambda: ix.partitioned_inlj(d_pr, positions=False, pairs=True)[1:]}
+    for o, run in runs.items():
+        out, cnt = run()
+        rows, pos = pairs_of(out, cnt)
+        order_ = np.argsort(rows, kind="stable")
+        np.testing.assert_array_equal(rows[order_], erows, err_msg=f"order {o}")
+        np.testing.assert_array_equal(pos[order_], epos, err_msg=f"order {o}")
