@@ -258,7 +258,14 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_scatter_lookup(const
 // k_compact_pairs turns them into pairs.  The search pass has no block
 // barriers, and the compaction is a streaming pass.  Probes of a partitioned
 // relation (row ids, appended behind *d_base) take the single-pass k_pairs.
-constexpr int kItems = GJ_LOOKUP_ITEMS;          // k_pairs items per thread
+// k_pairs items per thread (8 measured fastest for gj_inlj_pairs_host, whose
+// tiles read their probes from and write their pairs to host memory: 15.2 ms
+// per 2^28 probes, against 18.7 with 4 and 21.4 with 16); GJ_PAIRS_ITEMS
+// overrides it in tuning builds
+#ifndef GJ_PAIRS_ITEMS
+#define GJ_PAIRS_ITEMS GJ_LOOKUP_ITEMS
+#endif
+constexpr int kItems = GJ_PAIRS_ITEMS;
 constexpr int kCompactItems = 16;                // k_compact_pairs items per thread
 static_assert(kItems >= 4 && (kItems & (kItems - 1)) == 0, "the pairs scan needs a power-of-two item count >= 4");
 constexpr uint32_t kTile = kBlock * kItems;
@@ -425,6 +432,7 @@ __device__ __forceinline__ uint32_t claim_tile(const pairs_ws& ws) {
     return s_tile;
 }
 
+
 // single pass: search and compact tile by tile (partitioned relations, whose
 // pairs are appended behind *d_base)
 template <class Op>
@@ -445,10 +453,10 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const __grid_c
             s_pos[k * kBlock + threadIdx.x] = i < m ? op(cache, key) : kInvalid;
         }
     };
+    auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
     for (;;) {
         const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
-        auto row_of = [&](int, uint64_t i) { return rows ? __ldcs(rows + i) : (uint32_t)i; };
         if (!pairs_tile<kItems>(search, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
     }
 }
