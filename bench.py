@@ -769,7 +769,7 @@ def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind
     else:
         bits, window, tuned_ms = gj.autotune_partitioned(ix, probes)
         tune = {"radix_bits": bits, "window": window, "ms": round(tuned_ms, 3),
-                "candidates": "fanout 2^8..2^12 x window {m, m/4, m/16}"}
+                "candidates": "fanout 2^5..2^12 x window {m, m/4, m/16}"}
     need = ctypes.c_size_t()
     gj._check(gj.lib().gj_partitioned_inlj_workspace_size(ix.handle, window, bits, ctypes.byref(need)))
     ws = torch.empty(need.value, dtype=torch.uint8, device=device)
@@ -847,9 +847,8 @@ def partitioned_measure(args, world, device, stream, n_log2, m_log2, steps, kind
 
 def partitioned_workload(args, world, rank, device, stream):
     """Partitioned INLJ at out-of-L2 scale: 2^28-key index, 2^29 Zipf(0.5)
-    probes, range partition with an autotuned fanout (2^8..2^12) and window."""
-    n_log2 = args.n_log2 if args.n_log2 != 26 else 28
-    m_log2 = args.m_log2 if args.m_log2 != 28 else 29
+    probes, range partition with an autotuned fanout (2^5..2^12) and window."""
+    n_log2, m_log2 = args.n_log2, args.m_log2
     kind = args.indexes.split(",")[0]
     r = partitioned_measure(args, world, device, stream, n_log2, m_log2, args.steps, kind)
     return _base_line(
@@ -1177,7 +1176,7 @@ def learned_measure(args, world, device, stream, n_log2, m_log2, steps, quick):
 
 
 def learned_workload(args, world, rank, device, stream):
-    n_log2 = args.n_log2 if args.n_log2 != 26 else 27
+    n_log2 = args.n_log2
     results, parity = learned_measure(args, world, device, stream, n_log2, args.m_log2, args.steps, args.learned_quick)
     head = results["uniform"]["learned"]
     n, m = 1 << n_log2, 1 << args.m_log2
@@ -1335,8 +1334,10 @@ def parse_args(argv=None):
     ap.add_argument("--workload", choices=["inlj", "partitioned", "star", "learned", "batch", "host_index",
                                            "orderings"], default="inlj")
     ap.add_argument("--host-n-log2", default="26,28", help="host_index: column sizes (log2 keys)")
-    ap.add_argument("--n-log2", type=int, default=26)
-    ap.add_argument("--m-log2", type=int, default=28)
+    ap.add_argument("--n-log2", type=int, default=None,
+                    help="build keys (log2); default 26, 28 for partitioned, 27 for learned")
+    ap.add_argument("--m-log2", type=int, default=None,
+                    help="probes (log2); default 28, 29 for partitioned")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--indexes", default="btree,harmonia,radix_spline,binary_search,learned,hash,btree_w64")
     ap.add_argument("--seed", type=int, default=20261203)
@@ -1373,8 +1374,17 @@ def parse_args(argv=None):
     return ap.parse_args(argv)
 
 
+# (build keys, probes) as log2 per workload when not given
+SIZES = {"partitioned": (28, 29), "learned": (27, 28)}
+
+
 def main(argv=None):
     args = parse_args(argv)
+    n_def, m_def = SIZES.get(args.workload, (26, 28)) if args.impl != "reference" else (26, 28)
+    if args.n_log2 is None:
+        args.n_log2 = n_def
+    if args.m_log2 is None:
+        args.m_log2 = m_def
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

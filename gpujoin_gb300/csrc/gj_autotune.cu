@@ -74,12 +74,14 @@ int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uin
     GJ_CHECK_ARG(index && radix_bits && window_size, "gj_autotune_partitioned: null argument");
     GJ_CHECK_ARG(m > 0 && d_probes, "gj_autotune_partitioned: no probes");
     cudaStream_t s = as_stream(stream);
-    // candidates: fanout 2^8 .. 2^12; window = all probes, a quarter, a sixteenth
+    // candidates: fanout 2^5 .. 2^12 (the best partitions hold about 2^21
+    // keys: measured 2^5 at 2^26 keys, 2^7-2^8 at 2^28); window = all
+    // probes, a quarter, a sixteenth
     std::vector<uint64_t> windows = {m};
     if (m >= (4u << 20)) windows.push_back(m / 4);
     if (m >= (16u << 20)) windows.push_back(m / 16);
     size_t ws_max = 0;
-    for (uint32_t bits = 8; bits <= 12; ++bits)
+    for (uint32_t bits = 5; bits <= 12; ++bits)
         for (uint64_t w : windows) {
             size_t need = 0;
             GJ_TRY(gj_partitioned_inlj_workspace_size(index, w, bits, &need));
@@ -92,7 +94,7 @@ int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uin
     event_pair ev;
     GJ_TRY(ev.init());
     float best = -1.f;
-    for (uint32_t bits = 8; bits <= 12; ++bits)
+    for (uint32_t bits = 5; bits <= 12; ++bits)
         for (uint64_t w : windows) {
             float t = 0.f;
             GJ_TRY(time_best(

@@ -168,7 +168,7 @@ size_t partition_ws_bytes(uint64_t m, uint32_t radix_bits, int sm_count);
 int range_partition_impl(const uint64_t* d_keys, uint64_t m, uint64_t min_key, uint32_t shift, uint32_t radix_bits,
                          uint64_t row_base, uint64_t* d_out_keys, uint32_t* d_out_rows, uint64_t* d_offsets, void* ws,
                          size_t ws_bytes, cudaStream_t s);
-// fanout for an index of n keys (about 2^20 keys a partition, 2^8..2^12)
+// fanout for an index of n keys (about 2^21 keys a partition, 2^5..2^12)
 uint32_t default_radix_bits(uint64_t n);
 // smallest shift that maps [min_key, max_key] onto 2^radix_bits partitions
 uint32_t shift_for(uint64_t min_key, uint64_t max_key, uint32_t radix_bits);

@@ -47,7 +47,13 @@ int device_alloc_for(gj_index* idx, size_t bytes, void** out);  // gj_index.cu
 namespace {
 
 constexpr uint32_t kMaxRadixBits = 12;
-constexpr uint32_t kMaxDirBits = 28;       // at most 2^28 buckets (1 GiB of entries)
+// at most 2^28 buckets (1 GiB of entries); GJ_MAX_DIR_BITS overrides it in
+// tuning builds (at most 31)
+#ifndef GJ_MAX_DIR_BITS
+#define GJ_MAX_DIR_BITS 28
+#endif
+constexpr uint32_t kMaxDirBits = GJ_MAX_DIR_BITS;
+static_assert(kMaxDirBits <= 31, "bucket indexes and the closing entry fit 32 bits");
 constexpr int kDirBlock = 256;
 constexpr int kDirPer = 8;                 // column positions (and directory entries) per thread
 constexpr int kScanBlock = 1024;

@@ -424,7 +424,7 @@ int gj_batch_plan_autotune(gj_batch_plan* plan, const uint64_t* d_probes, uint32
  * synchronise: set-up calls, not part of the probe path.  No counterpart in
  * the reference, whose experiment_config takes these values as options
  * (src/index_lookup_config.hpp:18-37).
- *   partitioned INLJ (pairs): fanout 2^8..2^12 x window {m, m/4, m/16};
+ *   partitioned INLJ (pairs): fanout 2^5..2^12 x window {m, m/4, m/16};
  *   B+tree lookups: node width {4, 7 (compressed), 8, 15 (compressed), 16} x leaf width {4, 8, 16, 32}. */
 int gj_autotune_partitioned(const gj_index* index, const uint64_t* d_probes, uint64_t m, void* stream,
                             uint32_t* radix_bits, uint64_t* window_size, float* best_ms);
