@@ -32,7 +32,7 @@ def test_autotune_partitioned(orc, gj, cuda):
     ix = gj.btree_index().construct(None, d_col)
     bits, window, ms = gj.autotune_partitioned(ix, d_pr)
     m = len(pr)
-    assert 8 <= bits <= 12 and window in (m, m // 4, m // 16) and ms > 0
+    assert 5 <= bits <= 12 and window in (m, m // 4, m // 16) and ms > 0
     _, prs, cnt = ix.partitioned_inlj(d_pr, window_size=window, radix_bits=bits, positions=False, pairs=True)
     rows, bpos = pairs_of(prs, cnt)
     erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
@@ -50,7 +50,7 @@ def test_autotune_partitioned_btree(orc, gj, cuda):
     d_col, d_pr = to_dev(torch, col), to_dev(torch, pr)
     w, lk, bits, window, ms = gj.autotune_partitioned_btree(d_col, d_pr)
     m = len(pr)
-    assert (w, lk) in ((4, 4), (4, 8), (4, 16), (7, 4), (15, 4)) and 8 <= bits <= 12 and window in (m, m // 4, m // 16)
+    assert (w, lk) in ((4, 4), (4, 8), (4, 16), (7, 4), (15, 4)) and 5 <= bits <= 12 and window in (m, m // 4, m // 16)
     ix = gj.btree_index(btree_node_keys=w, btree_leaf_keys=lk).construct(None, d_col)
     _, prs, cnt = ix.partitioned_inlj(d_pr, window_size=window, radix_bits=bits, positions=False, pairs=True)
     rows, bpos = pairs_of(prs, cnt)
