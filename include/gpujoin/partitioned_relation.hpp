@@ -7,6 +7,7 @@
 //   get_experiment_config, radix_bits            src/index_lookup_config.hpp:18-72,
 //                                                src/index_lookup_config.cpp:31-97
 //   device_array_wrapper, create_device_array    src/device_array.hpp:132-236
+//   inlj_pairs_by_approach                       src/index_lookup_new.cu:302-308
 //
 // Code written against the reference keeps its shape:
 //
@@ -244,4 +245,64 @@ inline bool parse_options(int argc, char** argv) {
         }
     }
     return false;
+}
+
+// ---------------------------------------------------------------------------
+// approaches (the reference's approach map, src/index_lookup_new.cu:302-308)
+// ---------------------------------------------------------------------------
+// The join pairs of m probes against index by config.approach:
+//   "plain"         gj_inlj_pairs (plain_approach): pairs in probe order
+//   "bws"           gj_inlj_pairs_sorted (blockwise_sorting_approach): tile by
+//                   tile in probe order, key order inside a tile
+//   "partitioning"  gj_partitioned_inlj (partitioning_approach): windows of
+//                   config.partitioning_approach_window_size probes (0: all),
+//                   the library's default fanout; pairs grouped by partition
+//                   tile
+//   "auto"          whichever of the three gj_autotune_ordering times fastest
+//                   on these probes
+// Every approach gives the same set of pairs.  The reference's "hj" (its hash
+// join) is an index kind here (GJ_INDEX_HASH), joined by any of them.
+// d_pairs (2m u32: probe row, build position) and d_count (one u64) are device
+// memory.  Unknown approach names throw std::invalid_argument, library errors
+// std::runtime_error.  Workspaces are allocated and freed here, so the call
+// synchronises the stream.
+static const uint32_t approach_auto = 0xFFFFFFFFu;
+
+// the GJ_ORDER_* of an approach name, approach_auto for "auto"
+inline uint32_t approach_order(const std::string& a) {
+    if (a == "plain") return GJ_ORDER_PROBE;
+    if (a == "bws") return GJ_ORDER_SORTED_TILES;
+    if (a == "partitioning") return GJ_ORDER_PARTITIONED;
+    if (a == "auto") return approach_auto;
+    throw std::invalid_argument("unknown approach " + a);
+}
+
+template <class Index>
+void inlj_pairs_by_approach(const Index& index, const uint64_t* d_probes, size_t m, uint32_t* d_pairs,
+                            uint64_t* d_count, const experiment_config& config = get_experiment_config(),
+                            cudaStream_t stream = nullptr) {
+    const gj_index* ix = index.handle.get();
+    uint32_t order = approach_order(config.approach);
+    if (order == approach_auto) {
+        order = GJ_ORDER_PROBE;
+        if (m > 0) gj::detail::check_rc(gj_autotune_ordering(ix, d_probes, m, stream, &order, nullptr));
+    }
+    if (order == GJ_ORDER_PARTITIONED) {
+        const uint64_t w = config.partitioning_approach_window_size ? config.partitioning_approach_window_size
+                                                                    : (m ? m : 1);
+        size_t need = 0;
+        gj::detail::check_rc(gj_partitioned_inlj_workspace_size(ix, w, 0, &need));
+        device_array_wrapper<unsigned char> ws(need);
+        gj::detail::check_rc(
+            gj_partitioned_inlj(ix, d_probes, m, w, 0, nullptr, d_pairs, d_count, ws.data(), need, stream));
+    } else {
+        size_t need = 0;
+        gj::detail::check_rc(gj_inlj_pairs_workspace_size(m, &need));
+        device_array_wrapper<unsigned char> ws(need);
+        gj::detail::check_rc(order == GJ_ORDER_SORTED_TILES
+                                 ? gj_inlj_pairs_sorted(ix, d_probes, m, d_pairs, d_count, ws.data(), need, stream)
+                                 : gj_inlj_pairs(ix, d_probes, m, d_pairs, d_count, ws.data(), need, stream));
+    }
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        throw std::runtime_error("inlj_pairs_by_approach: stream failed");
 }

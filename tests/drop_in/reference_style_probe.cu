@@ -153,6 +153,51 @@ extern "C" int drop_in_partitioned_probe(int kind, const index_key_t* d_col, con
     }
 }
 
+// the join pairs by the reference's approach names (inlj_pairs_by_approach
+// with experiment_config::approach set from the command line's -a); 0, or 4
+// for an unknown approach, 1 for a library error
+template <class IndexType>
+static int run_approach(const char* approach, uint64_t window, const index_key_t* d_col, const index_key_t* h_col,
+                        uint64_t n, const index_key_t* d_keys, uint64_t m, uint32_t* d_pairs, uint64_t* d_count) {
+    IndexType index;
+    index.construct(vector_view<index_key_t>(const_cast<index_key_t*>(h_col), n), d_col);
+    experiment_config config;
+    config.approach = approach;
+    config.partitioning_approach_window_size = window;
+    try {
+        inlj_pairs_by_approach(index, d_keys, m, d_pairs, d_count, config);
+    } catch (const std::invalid_argument&) {
+        return 4;
+    }
+    return 0;
+}
+
+// 1 when approach_order knows the name, 0 when it throws
+extern "C" int drop_in_approach_name_known(const char* approach) {
+    try {
+        approach_order(approach);
+        return 1;
+    } catch (const std::invalid_argument&) {
+        return 0;
+    }
+}
+
+extern "C" int drop_in_approach_pairs(int kind, const char* approach, uint64_t window, const index_key_t* d_col,
+                                      const index_key_t* h_col, uint64_t n, const index_key_t* d_keys, uint64_t m,
+                                      uint32_t* d_pairs, uint64_t* d_count) {
+    try {
+        if (kind == 0)
+            return run_approach<btree_index<index_key_t, value_t>>(approach, window, d_col, h_col, n, d_keys, m,
+                                                                   d_pairs, d_count);
+        if (kind == 2)
+            return run_approach<binary_search_index<index_key_t, value_t>>(approach, window, d_col, h_col, n, d_keys,
+                                                                           m, d_pairs, d_count);
+        return 3;
+    } catch (const std::exception&) {
+        return 1;
+    }
+}
+
 // parse_options on a reference-style command line; out[] = the parsed
 // fields, return 0, 1 when -h was given, -1 when parsing threw
 extern "C" int drop_in_parse_options(int argc, char** argv, uint64_t* out, char* approach, char* index) {

@@ -142,3 +142,49 @@ def test_reference_style_partitioned_probe(tmp_path, orc, gj, cuda, kind, bits):
     got = out.cpu().numpy().view(np.uint32)
     exp = orc.exact_lookup(col, pr) if kind == 0 else orc.bs_lookup(col, pr)
     np.testing.assert_array_equal(got, exp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,name", [(0, "btree"), (2, "binary_search")])
+@pytest.mark.parametrize("approach,window", [("plain", 0), ("bws", 0), ("partitioning", 10000), ("partitioning", 0),
+                                             ("auto", 0)])
+def test_reference_style_approaches(tmp_path, orc, gj, cuda, kind, name, approach, window):
+    # inlj_pairs_by_approach: the reference's approach names give the same
+    # set of pairs; "plain" gives them in probe order
+    import torch
+
+    lib = ctypes.CDLL(build_drop_in(tmp_path))
+    lib.drop_in_approach_pairs.restype = ctypes.c_int
+    lib.drop_in_approach_pairs.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                           ctypes.c_void_p, ctypes.c_void_p]
+    rng = np.random.default_rng(kind * 10 + len(approach) + window)
+    col = np.sort(np.unique(rng.integers(0, 1 << 63, 70000, dtype=np.uint64)))[:65536]
+    pr = np.concatenate([col[rng.integers(0, len(col), 30000)], rng.integers(0, 1 << 63, 7001, dtype=np.uint64)])
+    rng.shuffle(pr)
+    d_col = torch.from_numpy(col.view(np.int64)).cuda()
+    d_pr = torch.from_numpy(pr.view(np.int64)).cuda()
+    pairs = torch.empty(2 * len(pr), dtype=torch.int32, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    rc = lib.drop_in_approach_pairs(kind, approach.encode(), window, d_col.data_ptr(), col.ctypes.data, len(col),
+                                    d_pr.data_ptr(), len(pr), pairs.data_ptr(), count.data_ptr())
+    assert rc == 0
+    c = int(count.item())
+    got = pairs[: 2 * c].cpu().numpy().view(np.uint32).reshape(-1, 2)
+    exp = orc.exact_lookup(col, pr) if name == "btree" else orc.bs_lookup(col, pr)
+    erows, epos = orc.pairs_from_positions(exp)
+    if approach == "plain":
+        np.testing.assert_array_equal(got[:, 0], erows)
+        np.testing.assert_array_equal(got[:, 1], epos)
+    order = np.argsort(got[:, 0], kind="stable")
+    np.testing.assert_array_equal(got[order, 0], erows)
+    np.testing.assert_array_equal(got[order, 1], epos)
+
+
+def test_reference_style_unknown_approach(tmp_path, gj):
+    # an unknown approach name is refused before anything runs on a GPU
+    lib = ctypes.CDLL(build_drop_in(tmp_path))
+    lib.drop_in_approach_name_known.restype = ctypes.c_int
+    lib.drop_in_approach_name_known.argtypes = [ctypes.c_char_p]
+    assert [lib.drop_in_approach_name_known(a) for a in (b"plain", b"bws", b"partitioning", b"auto")] == [1] * 4
+    assert lib.drop_in_approach_name_known(b"hj") == 0 and lib.drop_in_approach_name_known(b"sorted") == 0
