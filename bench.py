@@ -1378,13 +1378,19 @@ def parse_args(argv=None):
 SIZES = {"partitioned": (28, 29), "learned": (27, 28)}
 
 
-def main(argv=None):
-    args = parse_args(argv)
+def resolve_sizes(args):
+    """Fill in the build and probe sizes a workload runs at when not given
+    (the reference arm runs the INLJ sizes)."""
     n_def, m_def = SIZES.get(args.workload, (26, 28)) if args.impl != "reference" else (26, 28)
     if args.n_log2 is None:
         args.n_log2 = n_def
     if args.m_log2 is None:
         args.m_log2 = m_def
+    return args
+
+
+def main(argv=None):
+    args = resolve_sizes(parse_args(argv))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

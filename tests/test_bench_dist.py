@@ -80,3 +80,21 @@ def test_bench_defines_each_function_once():
     tree = ast.parse(open(path).read())
     names = collections.Counter(n.name for n in tree.body if isinstance(n, ast.FunctionDef))
     assert not [k for k, v in names.items() if v > 1]
+
+
+def test_workload_sizes():
+    # each workload's default sizes (log2 keys, log2 probes), and explicit sizes kept
+    sys.path.insert(0, ROOT)
+    import bench
+
+    def sizes(*argv):
+        a = bench.resolve_sizes(bench.parse_args(list(argv)))
+        return a.n_log2, a.m_log2
+
+    assert sizes() == (26, 28)
+    assert sizes("--workload", "partitioned") == (28, 29)
+    assert sizes("--workload", "learned") == (27, 28)
+    assert sizes("--workload", "orderings") == (26, 28)
+    assert sizes("--impl", "reference") == (26, 28)
+    assert sizes("--workload", "partitioned", "--n-log2", "26", "--m-log2", "28") == (26, 28)
+    assert sizes("--workload", "learned", "--n-log2", "20") == (20, 28)
