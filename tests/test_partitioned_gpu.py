@@ -62,7 +62,9 @@ def test_partitioned_directory_cases(orc, gj, cuda, kind, case, prepared):
         ix.prepare_partitioned()
     exp = expected(orc, kind, col, pr)
     erows, epos = orc.pairs_from_positions(exp)
-    for bits, window in ((8, 0), (12, 0), (10, 7777)):
+    # the wide scatter (fanout 2^8 and up), the narrow one (below 2^8), and the
+    # default fanout (0: about 2^20 keys a partition, from 2^5)
+    for bits, window in ((8, 0), (12, 0), (10, 7777), (5, 0), (6, 20000), (0, 0)):
         pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=bits, positions=True,
                                             pairs=True)
         got = from_dev_u32(pos)
@@ -95,7 +97,7 @@ def test_partitioned_skewed_probes(orc, gj, cuda, kind):
     for prepared in (False, True):
         if prepared:
             ix.prepare_partitioned()
-        for bits, window in ((8, 0), (11, 0), (8, 65536)):
+        for bits, window in ((8, 0), (11, 0), (8, 65536), (5, 0), (7, 65536)):
             pos, prs, cnt = ix.partitioned_inlj(to_dev(torch, pr), window_size=window, radix_bits=bits,
                                                 positions=True, pairs=True)
             np.testing.assert_array_equal(from_dev_u32(pos), exp, err_msg=f"{kind}/2^{bits}/{window}")
