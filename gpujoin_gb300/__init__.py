@@ -140,6 +140,7 @@ _SIGNATURES = {
     "gj_debug_inlj_pairs_stalled": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _u32, _vp]),
     "gj_inlj_pairs_host_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_inlj_pairs_host_unordered": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_noalloc": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp]),
     "gj_partition_workspace_size": (_i32, [_u64, _u32, ctypes.POINTER(_sz)]),
     "gj_index_key_range": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
@@ -403,16 +404,18 @@ class abstract_index:
                                           ctypes.byref(o), ctypes.byref(ms)))
         return o.value, ms.value
 
-    def inlj_pairs_host(self, h_probes, h_pairs, h_count, workspace=None, stream=None):
+    def inlj_pairs_host(self, h_probes, h_pairs, h_count, workspace=None, stream=None, ordered: bool = True):
         """inlj_pairs on pinned HOST tensors (probes int64, pairs int32 of 2m, count int64 of 1): the
-        kernels read and write host memory directly; the result is valid after the stream syncs."""
+        kernels read and write host memory directly; the result is valid after the stream syncs.
+        ordered=False: the same pairs in the order their tiles finish (gj_inlj_pairs_host_unordered)."""
         m = h_probes.numel()
         if workspace is None:
             need = _sz(0)
             _check(lib().gj_inlj_pairs_host_workspace_size(m, ctypes.byref(need)))
             workspace = _workspace(need.value, _torch().device("cuda", _torch().cuda.current_device()))
-        _check(lib().gj_inlj_pairs_host(self.handle, _hptr(h_probes), m, _hptr(h_pairs), _hptr(h_count),
-                                        _ptr(workspace), workspace.numel(), _stream(stream)))
+        fn = lib().gj_inlj_pairs_host if ordered else lib().gj_inlj_pairs_host_unordered
+        _check(fn(self.handle, _hptr(h_probes), m, _hptr(h_pairs), _hptr(h_count), _ptr(workspace), workspace.numel(),
+                  _stream(stream)))
         return h_pairs, h_count
 
     @staticmethod

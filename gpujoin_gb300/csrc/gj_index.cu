@@ -981,31 +981,55 @@ int gj_inlj_pairs_host_workspace_size(uint64_t m, size_t* bytes) {
     return GJ_OK;
 }
 
-int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
-                       uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream) {
-    GJ_CHECK_ARG(index && h_count, "gj_inlj_pairs_host: null argument");
-    GJ_CHECK_ARG(m == 0 || (h_probes && h_pairs), "gj_inlj_pairs_host: null buffer");
+// gj_inlj_pairs_host and gj_inlj_pairs_host_unordered (name: the entry
+// point, for the error messages)
+static int host_pairs(const char* name, bool ordered, const gj_index* index, const uint64_t* h_probes, uint64_t m,
+                      uint32_t* h_pairs, uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    if (!index || !h_count) {
+        set_error("%s: null argument", name);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
+    if (m != 0 && (!h_probes || !h_pairs)) {
+        set_error("%s: null buffer", name);
+        return GJ_ERR_INVALID_ARGUMENT;
+    }
     if (m > (uint64_t)UINT32_MAX) {
-        set_error("gj_inlj_pairs_host: probe rows must fit 32 bits");
+        set_error("%s: probe rows must fit 32 bits", name);
         return GJ_ERR_TOO_LARGE;
     }
+    const std::string what = name;
     void *probes = nullptr, *pairs = nullptr, *count = nullptr;
-    GJ_TRY(device_address(h_count, "gj_inlj_pairs_host: count", &count));
+    GJ_TRY(device_address(h_count, (what + ": count").c_str(), &count));
     if (m == 0) {
         // nothing to launch: the count is written once earlier work on the stream is done
         GJ_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
         *h_count = 0;
         return GJ_OK;
     }
-    GJ_TRY(device_address(h_probes, "gj_inlj_pairs_host: probes", &probes));
-    GJ_TRY(device_address(h_pairs, "gj_inlj_pairs_host: pairs", &pairs));
+    GJ_TRY(device_address(h_probes, (what + ": probes").c_str(), &probes));
+    GJ_TRY(device_address(h_pairs, (what + ": pairs").c_str(), &pairs));
     // One pass: each tile reads its probes from host memory, searches them
     // and writes its pairs back, so host-link reads, searches and writes of
     // different tiles overlap (a separate compaction pass would serialise
     // the writes behind the searches).
+    if (!ordered)
+        return launch_pairs_unordered(index, static_cast<const uint64_t*>(probes), m, static_cast<uint32_t*>(pairs),
+                                      static_cast<uint64_t*>(count), d_workspace, workspace_bytes, as_stream(stream));
     return launch_pairs(index, static_cast<const uint64_t*>(probes), m, nullptr, static_cast<uint32_t*>(pairs),
                         nullptr, static_cast<uint64_t*>(count), d_workspace, workspace_bytes, nullptr,
                         as_stream(stream));
+}
+
+int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
+                       uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    return host_pairs("gj_inlj_pairs_host", true, index, h_probes, m, h_pairs, h_count, d_workspace, workspace_bytes,
+                      stream);
+}
+
+int gj_inlj_pairs_host_unordered(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
+                                 uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    return host_pairs("gj_inlj_pairs_host_unordered", false, index, h_probes, m, h_pairs, h_count, d_workspace,
+                      workspace_bytes, stream);
 }
 
 int gj_inlj_pairs_status(const void* d_workspace, size_t workspace_bytes, uint64_t m, void* stream) {

@@ -158,6 +158,10 @@ size_t pairs_workspace_bytes(uint64_t m);
 // spin_limit polls, and tile 0 is never claimed (so every wait runs out)
 int launch_pairs_stalled(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                          uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t spin_limit, cudaStream_t s);
+// launch_pairs in one pass with each tile's pairs placed by one atomicAdd
+// (in the order tiles finish) instead of in probe order; the same set
+int launch_pairs_unordered(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                           uint64_t* d_count, void* ws, size_t ws_bytes, cudaStream_t s);
 int pairs_error_flag(void* ws, size_t ws_bytes, uint64_t m, unsigned int* flag, cudaStream_t s);
 
 // range partition of probe keys (gj_partition.cu): partition(k) =

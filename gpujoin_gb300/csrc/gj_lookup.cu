@@ -30,7 +30,7 @@ int dispatch(const gj_index* idx, const lookup_call& c) {
 
 size_t pairs_workspace_bytes(uint64_t m) {
     const uint64_t states = (m + kStateTile - 1) / kStateTile;
-    return workspace_carver::need({(size_t)(states ? states : 1) * 8, 8});
+    return workspace_carver::need({(size_t)(states ? states : 1) * 8, 8, 16});
 }
 
 int launch_lookup(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_out, cudaStream_t s) {
@@ -71,6 +71,13 @@ int launch_pairs_stalled(const gj_index* idx, const uint64_t* d_probes, uint64_t
                   d_pairs ? d_pairs + m : nullptr, s};
     c.spin_limit = spin_limit;
     c.skip_first_tile = true;
+    return dispatch(idx, c);
+}
+
+int launch_pairs_unordered(const gj_index* idx, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                           uint64_t* d_count, void* ws, size_t ws_bytes, cudaStream_t s) {
+    lookup_call c{lookup_action::pairs, d_probes, nullptr, m, d_pairs, nullptr, d_count, ws, ws_bytes, nullptr, s};
+    c.unordered = true;
     return dispatch(idx, c);
 }
 

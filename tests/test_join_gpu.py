@@ -199,10 +199,12 @@ def test_star_join_full_window_and_empty_window(orc, gj, cuda):
             assert (int(got[0]), int(got[1])) == (num, den), (lo, hi, sorted_batches)
 
 
+@pytest.mark.parametrize("ordered", [True, False])
 @pytest.mark.parametrize("kind", ["btree", "radix_spline", "learned"])
 @pytest.mark.parametrize("m", [0, 1, 4097, 300001])
-def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m):
-    # probes, pairs and count in pinned host memory, read and written by the kernels
+def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m, ordered):
+    # probes, pairs and count in pinned host memory, read and written by the
+    # kernels; unordered: the same set of pairs, tiles in the order they finish
     import torch
 
     rng = np.random.default_rng(m + 11)
@@ -212,19 +214,22 @@ def test_inlj_pairs_host_buffers(orc, gj, cuda, kind, m):
     h_pr = torch.from_numpy(pr.view(np.int64).copy()).pin_memory()
     h_pairs = torch.full((2 * max(m, 1),), -1, dtype=torch.int32).pin_memory()
     h_cnt = torch.full((1,), -1, dtype=torch.int64).pin_memory()
-    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt)
+    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt, ordered=ordered)
     torch.cuda.synchronize()
     c = int(h_cnt[0])
     got = h_pairs[: 2 * c].numpy().view(np.uint32).reshape(-1, 2)
     erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
+    if not ordered:
+        got = got[np.argsort(got[:, 0], kind="stable")]
     np.testing.assert_array_equal(got[:, 0], erows)
     np.testing.assert_array_equal(got[:, 1], epos)
 
 
+@pytest.mark.parametrize("ordered", [True, False])
 @pytest.mark.parametrize("m", [(1 << 24) + 54321, 3 * (1 << 24) + 5])
-def test_inlj_pairs_host_buffers_large(orc, gj, cuda, m):
-    # tens of millions of probes from host buffers: every pair in probe
-    # order, the status reads clean
+def test_inlj_pairs_host_buffers_large(orc, gj, cuda, m, ordered):
+    # tens of millions of probes from host buffers: every pair (in probe
+    # order unless unordered), the status reads clean
     import torch
 
     rng = np.random.default_rng(3)
@@ -238,12 +243,14 @@ def test_inlj_pairs_host_buffers_large(orc, gj, cuda, m):
     need = ctypes.c_size_t(0)
     gj.lib().gj_inlj_pairs_host_workspace_size(m, ctypes.byref(need))
     ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
-    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt, ws)
+    ix.inlj_pairs_host(h_pr, h_pairs, h_cnt, ws, ordered=ordered)
     torch.cuda.synchronize()
     ix.inlj_pairs_status(ws, m)
     c = int(h_cnt[0])
     got = h_pairs[: 2 * c].numpy().view(np.uint32).reshape(-1, 2)
     erows, epos = orc.pairs_from_positions(orc.exact_lookup(col, pr))
+    if not ordered:
+        got = got[np.argsort(got[:, 0], kind="stable")]
     np.testing.assert_array_equal(got[:, 0], erows)
     np.testing.assert_array_equal(got[:, 1], epos)
 
