@@ -632,7 +632,8 @@ def inlj_workload(args, world, rank, device, stream):
         c_ms = time_steps(copy_step, e_steps, args.warmup, stream, world, device)
         c_ms = max_over_ranks(c_ms, world, device)
         # the same pairs in the order their tiles finish (no tile waits for
-        # its predecessors' counts), checked as a set against the oracle
+        # its predecessors' counts), checked as a set against the oracle;
+        # and the same from device buffers (gj_inlj_pairs_unordered)
         u_ms = time_steps(lambda: headline_ix.inlj_pairs_host(h_probes, h_pairs, h_count, hws, ordered=False),
                           e_steps, args.warmup, stream, world, device)
         u_ms = max_over_ranks(u_ms, world, device)
@@ -647,12 +648,27 @@ def inlj_workload(args, world, rank, device, stream):
             u_parity = {"checked": m, "mismatches": int((by_row != expect[sem]).sum().item()),
                         "semantics": sem + ", pairs as a set (rows placed by row id)"}
             del d_p, by_row
+        d_ms = time_steps(lambda: headline_ix.inlj_pairs(probes, pairs, count, ws, ordered=False), args.steps,
+                          args.warmup, stream, world, device)
+        d_ms = max_over_ranks(d_ms, world, device)
+        d_count = int(count.item())
+        d_parity = None
+        if expect is not None:
+            d_p = pairs[: 2 * d_count].view(-1, 2)
+            by_row = torch.full((m,), -1, dtype=torch.int32, device=device)
+            by_row[d_p[:, 0].long()] = d_p[:, 1]
+            d_parity = {"checked": m, "mismatches": int((by_row != expect[sem]).sum().item())}
+            del d_p, by_row
         e2e = {"value": world * m * e_steps / (e_ms / 1e3), "unit": "probe tuples/s", "h2d_bytes_per_step": 8 * m,
                "d2h_bytes_per_step": 8 * m + 8, "api": "gj_inlj_pairs_host (pinned host probes, pairs and count)",
                "explicit_copies_value": world * m * e_steps / (c_ms / 1e3),
                "unordered": {"value": world * m * e_steps / (u_ms / 1e3),
                              "api": "gj_inlj_pairs_host_unordered (the same pairs, tiles in the order they finish)",
-                             "pairs": u_count, "parity": u_parity}}
+                             "pairs": u_count, "parity": u_parity,
+                             "device_buffers": {"value": world * m * args.steps / (d_ms / 1e3),
+                                                "ms_per_step": d_ms / args.steps,
+                                                "api": "gj_inlj_pairs_unordered (device buffers)",
+                                                "pairs": d_count, "parity": d_parity}}}
 
     # Roofline of the dominant kernel.  A pairs step is two launches: the
     # search pass (k_lookup: probe key in, one 32-byte leaf sector, u32

@@ -136,6 +136,7 @@ _SIGNATURES = {
     "gj_index_lookup": (_i32, [_vp, _vp, _u64, _vp, _vp]),
     "gj_inlj_pairs_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
     "gj_inlj_pairs": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
+    "gj_inlj_pairs_unordered": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _vp]),
     "gj_inlj_pairs_status": (_i32, [_vp, _sz, _u64, _vp]),
     "gj_debug_inlj_pairs_stalled": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _sz, _u32, _vp]),
     "gj_inlj_pairs_host_workspace_size": (_i32, [_u64, ctypes.POINTER(_sz)]),
@@ -342,8 +343,10 @@ class abstract_index:
         _check(lib().gj_index_lookup(self.handle, _ptr(d_probes), m, _ptr(out), _stream(stream)))
         return out
 
-    def inlj_pairs(self, d_probes, out_pairs=None, out_count=None, workspace=None, stream=None):
-        """(probe row, build pos) pairs of the matches, in probe order (ij_lookup_kernel)."""
+    def inlj_pairs(self, d_probes, out_pairs=None, out_count=None, workspace=None, stream=None,
+                   ordered: bool = True):
+        """(probe row, build pos) pairs of the matches, in probe order (ij_lookup_kernel);
+        ordered=False: the same pairs in the order their tiles finish (gj_inlj_pairs_unordered)."""
         torch = _torch()
         m = d_probes.numel()
         dev = d_probes.device
@@ -355,8 +358,9 @@ class abstract_index:
             need = _sz(0)
             _check(lib().gj_inlj_pairs_workspace_size(m, ctypes.byref(need)))
             workspace = _workspace(need.value, dev)
-        _check(lib().gj_inlj_pairs(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count),
-                                   _ptr(workspace), workspace.numel(), _stream(stream)))
+        fn = lib().gj_inlj_pairs if ordered else lib().gj_inlj_pairs_unordered
+        _check(fn(self.handle, _ptr(d_probes), m, _ptr(out_pairs), _ptr(out_count), _ptr(workspace),
+                  workspace.numel(), _stream(stream)))
         return out_pairs, out_count
 
     def lookup_cooperative(self, d_probes, degree=4, out=None, stream=None):

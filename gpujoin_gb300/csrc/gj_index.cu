@@ -917,6 +917,18 @@ int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, u
                         d_pairs ? d_pairs + m : nullptr, as_stream(stream));
 }
 
+int gj_inlj_pairs_unordered(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                            uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream) {
+    GJ_CHECK_ARG(index && d_count, "gj_inlj_pairs_unordered: null argument");
+    GJ_CHECK_ARG(m == 0 || (d_probes && d_pairs), "gj_inlj_pairs_unordered: null buffer");
+    if (m > (uint64_t)UINT32_MAX) {
+        set_error("gj_inlj_pairs_unordered: probe rows must fit 32 bits");
+        return GJ_ERR_TOO_LARGE;
+    }
+    return launch_pairs_unordered(index, d_probes, m, d_pairs, d_count, d_workspace, workspace_bytes,
+                                  as_stream(stream));
+}
+
 int gj_debug_inlj_pairs_stalled(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                                 uint64_t* d_count, void* d_workspace, size_t workspace_bytes, uint32_t spin_limit,
                                 void* stream) {

@@ -178,6 +178,13 @@ int gj_index_lookup(const gj_index* index, const uint64_t* d_probes, uint64_t m,
 int gj_inlj_pairs_workspace_size(uint64_t m, size_t* bytes);
 int gj_inlj_pairs(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
                   uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
+/* gj_inlj_pairs in one pass with each tile's pairs placed by one atomicAdd
+ * in the order tiles finish (as the reference's join kernels place theirs,
+ * src/tpch/tpch_14_ij.cu:371-407): the same set of pairs and count, no
+ * ordered compaction.  Same arguments and workspace; d_pairs holds 2*m
+ * uint32 and nothing is parked in it. */
+int gj_inlj_pairs_unordered(const gj_index* index, const uint64_t* d_probes, uint64_t m, uint32_t* d_pairs,
+                            uint64_t* d_count, void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* ---- warp-collective searches ---------------------------------------------- */
 /* gj_index_lookup with the reference's warp-collective search protocol:

@@ -16,17 +16,23 @@ def pairs_of(out_pairs, count):
     return a[:, 0].copy(), a[:, 1].copy()
 
 
+@pytest.mark.parametrize("ordered", [True, False])
 @pytest.mark.parametrize("kind", ["binary_search", "btree", "harmonia", "radix_spline", "hash"])
 @pytest.mark.parametrize("m", [0, 1, 31, 2047, 2048, 2049, 100003])
-def test_inlj_pairs_match_oracle(orc, gj, cuda, kind, m):
+def test_inlj_pairs_match_oracle(orc, gj, cuda, kind, m, ordered):
+    # in probe order, or (gj_inlj_pairs_unordered) the same set
     import torch
 
     rng = np.random.default_rng(m + 3)
     col = column(rng, 32 * 1000)
     pr = probes_for(rng, col, max(m, 1))[:m]
     ix = gj.make_index(kind).construct(None, to_dev(torch, col))
-    out, cnt = ix.inlj_pairs(to_dev(torch, pr) if m else torch.empty(0, dtype=torch.int64, device="cuda"))
+    out, cnt = ix.inlj_pairs(to_dev(torch, pr) if m else torch.empty(0, dtype=torch.int64, device="cuda"),
+                             ordered=ordered)
     rows, pos = pairs_of(out, cnt)
+    if not ordered:
+        order = np.argsort(rows, kind="stable")
+        rows, pos = rows[order], pos[order]
     erows, epos = orc.pairs_from_positions(expected(orc, kind, col, pr))
     np.testing.assert_array_equal(rows, erows)
     np.testing.assert_array_equal(pos, epos)
